@@ -1,0 +1,364 @@
+// ref_harness — runs the reference's own path tracer (Xitils headers) behind
+// the checker API of oracle/scene_api.h.
+//
+// TEST INFRASTRUCTURE ONLY. Built by oracle/build_ref.py into
+// oracle/_ref/libxref.so from a patched copy of the reference headers in
+// oracle/_ref/src (two mechanical g++ fixes; see build_ref.py) plus the shims
+// in oracle/shim. Nothing here is part of the product.
+//
+// Everything on the rendering path is the reference's code:
+//   TriangleMesh::setGeometry (TriangleMesh.h:151-161), Object (Object.h:32-34),
+//   Scene::addObject / buildAccelerationStructure (Scene.h:17-28),
+//   PinholeCamera (Camera.h:32-55), the materials (Material.h), SkySphereFromImage
+//   and SkySphereUniform (SkySphere.h), StandardPathTracer / NaivePathTracer
+//   (PathTracer.h), RenderTarget / RenderTargetTile (RenderTarget.h), and the
+//   sandbox materials GlossyClamped / MicrofacetNormalMapping extracted verbatim
+//   from Sandbox/MicrofacetBasedNormalMapping/Main.cpp:13-340.
+// The harness adds, through the reference's own virtual interfaces (the way
+// the sandboxes extend it):
+//   - PcgSampler: a Sampler whose protected virtual rand() (Sampler.h:74) draws
+//     from the per-(pixel, sample) PCG32 stream shared with the GPU path;
+//   - MetalRoughnessTexture: Metal (Material.h:275-384) whose roughness is read
+//     per hit from a texture (nearest lookup, red channel); every call builds a
+//     reference Metal with that roughness and delegates to it;
+//   - SkySphereLatLong: a lat-long environment map looked up with the
+//     reference's Texture::rgb (SkySphere.h:9-12 is a virtual interface).
+#include "cinder_prelude.h"
+
+#include <Xitils/AccelerationStructure.h>
+#include <Xitils/Camera.h>
+#include <Xitils/Geometry.h>
+#include <Xitils/Material.h>
+#include <Xitils/PathTracer.h>
+#include <Xitils/RenderTarget.h>
+#include <Xitils/Scene.h>
+#include <Xitils/SkySphere.h>
+#include <Xitils/TriangleMesh.h>
+#include <Xitils/VonMisesFisherDistribution.h>
+
+#include "mfnm_extract.h"
+
+#include <chrono>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "scene_api.h"
+
+using namespace xitils;
+
+namespace {
+
+uint64_t splitmix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+class PcgSampler : public _SamplerMersenneTwister {
+public:
+    PcgSampler() : _SamplerMersenneTwister(0) {}
+    void seedPath(uint32_t pixel, uint32_t sample, uint32_t seed) {
+        uint64_t initstate = splitmix64(((uint64_t)seed << 32) ^ (uint64_t)sample);
+        state = 0;
+        inc = ((uint64_t)pixel << 1) | 1u;
+        step();
+        state += initstate;
+        step();
+    }
+
+protected:
+    unsigned int rand() override { return step(); }
+
+private:
+    uint64_t state = 0, inc = 1;
+    uint32_t step() {
+        uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((-rot) & 31));
+    }
+};
+
+class MetalRoughnessTexture : public Material {
+public:
+    MetalRoughnessTexture(std::shared_ptr<Texture> rough, const Vector3f& f0) : rough(rough), f0(f0) {}
+    Vector3f bsdfCos(const SurfaceIntersection& isect, Sampler& sampler, const Vector3f& wi) const override {
+        return at(isect).bsdfCos(isect, sampler, wi);
+    }
+    Vector3f evalAndSample(const SurfaceIntersection& isect, Sampler& sampler, Vector3f* wi, float* pdf) const override {
+        return at(isect).evalAndSample(isect, sampler, wi, pdf);
+    }
+    float getPDF(const SurfaceIntersection& isect, const Vector3f& wi) const override { return at(isect).getPDF(isect, wi); }
+    Vector3f getAlbedo(const SurfaceIntersection& isect) const override { return f0; }
+
+private:
+    Metal at(const SurfaceIntersection& isect) const { return Metal(rough->rgb(isect.texCoord).x, f0); }
+    std::shared_ptr<Texture> rough;
+    Vector3f f0;
+};
+
+class SkySphereLatLong : public SkySphere {
+public:
+    explicit SkySphereLatLong(std::shared_ptr<Texture> tex) : tex(tex) {}
+    Vector3f getRadiance(const Vector3f& wi) override {
+        float u = atan2f(wi.x, -wi.z) * (0.5f / Pi) + 0.5f;
+        float cy = wi.y < -1.0f ? -1.0f : (wi.y > 1.0f ? 1.0f : wi.y);
+        float v = acosf(cy) * (1.0f / Pi);
+        return tex->rgb(Vector2f(u, v));
+    }
+
+private:
+    std::shared_ptr<Texture> tex;
+};
+
+struct RefScene {
+    Scene scene;
+    std::vector<std::shared_ptr<Texture>> textures;
+    std::vector<std::string> textureNames;
+    std::vector<std::shared_ptr<TriangleMesh>> meshes;
+    std::vector<std::shared_ptr<Material>> materials;
+    bool built = false;
+    int serial = 0;
+};
+
+int g_serial = 0;
+
+std::vector<Vector3f> toV3(const float* a, int n) {
+    std::vector<Vector3f> v(n);
+    for (int i = 0; i < n; ++i) v[i] = Vector3f(a[3 * i], a[3 * i + 1], a[3 * i + 2]);
+    return v;
+}
+
+Transform toTransform(const float* m, const float* mi) { return Transform(Matrix4x4(m), Matrix4x4(mi)); }
+
+}  // namespace
+
+extern "C" {
+ORC_DECLARE_SCENE_API(xref_)
+
+void* xref_scene_new(void) {
+    RefScene* s = new RefScene();
+    s->serial = ++g_serial;
+    return s;
+}
+void xref_scene_free(void* p) {
+    RefScene* s = (RefScene*)p;
+    for (auto& n : s->textureNames) stbi_mem_registry().erase(n);
+    delete s;
+}
+
+int xref_add_texture(void* p, int w, int h, const float* rgb, int wrap_clamp, int filter) {
+    RefScene* s = (RefScene*)p;
+    std::string name = "mem:" + std::to_string(s->serial) + ":" + std::to_string(s->textures.size());
+    stbi_mem_image img;
+    img.width = w; img.height = h;
+    img.rgb.assign(rgb, rgb + (size_t)w * h * 3);
+    stbi_mem_registry()[name] = std::move(img);
+    auto tex = std::make_shared<Texture>(name);  // Texture.h:17-23
+    tex->warpClamp = wrap_clamp != 0;
+    tex->filter = filter != 0;
+    s->textures.push_back(tex);
+    s->textureNames.push_back(name);
+    return (int)s->textures.size() - 1;
+}
+
+int xref_add_mesh(void* p, int nV, const float* pos, const float* uv, const float* nrm, const float* tan,
+                  const float* bit, int nIdx, const int32_t* idx) {
+    RefScene* s = (RefScene*)p;
+    std::vector<Vector3f> P = toV3(pos, nV), N, T, B;
+    std::vector<Vector2f> UV;
+    if (nrm) N = toV3(nrm, nV);
+    if (tan) T = toV3(tan, nV);
+    if (bit) B = toV3(bit, nV);
+    if (uv) { UV.resize(nV); for (int i = 0; i < nV; ++i) UV[i] = Vector2f(uv[2 * i], uv[2 * i + 1]); }
+    std::vector<int> I(idx, idx + nIdx);
+    auto mesh = std::make_shared<TriangleMesh>();
+    mesh->setGeometry(nV, P.data(), uv ? UV.data() : nullptr, nrm ? N.data() : nullptr, tan ? T.data() : nullptr,
+                      bit ? B.data() : nullptr, nIdx, I.data());
+    s->meshes.push_back(mesh);
+    return (int)s->meshes.size() - 1;
+}
+
+int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
+    RefScene* s = (RefScene*)p;
+    std::shared_ptr<Material> m;
+    switch (type) {
+    case ORC_MAT_DIFFUSE: {
+        auto d = std::make_shared<Diffuse>(Vector3f(f[0], f[1], f[2]));
+        if (tex >= 0) d->texture = s->textures[tex];
+        m = d;
+        break;
+    }
+    case ORC_MAT_METAL:
+        if (tex >= 0) m = std::make_shared<MetalRoughnessTexture>(s->textures[tex], Vector3f(f[1], f[2], f[3]));
+        else m = std::make_shared<Metal>(f[0], Vector3f(f[1], f[2], f[3]));
+        break;
+    case ORC_MAT_GLOSSY: m = std::make_shared<Glossy>(Vector3f(f[0], f[1], f[2]), f[3]); break;
+    case ORC_MAT_GLOSSY_CLAMPED: m = std::make_shared<GlossyClamped>(Vector3f(f[0], f[1], f[2]), f[3]); break;
+    case ORC_MAT_GLOSSY_HIGHLIGHT:
+        m = std::make_shared<GlossyWithHighLight>(Vector3f(f[0], f[1], f[2]), Vector3f(f[3], f[4], f[5]), f[6], f[7], f[8]);
+        break;
+    case ORC_MAT_EMISSION: m = std::make_shared<Emission>(Vector3f(f[0], f[1], f[2])); break;
+    case ORC_MAT_SPECULAR_REFLECTION: m = std::make_shared<SpecularReflection>(); break;
+    case ORC_MAT_SPECULAR_REFRACTION: {
+        auto r = std::make_shared<SpecularRefraction>();
+        r->index = f[0];
+        m = r;
+        break;
+    }
+    case ORC_MAT_SPECULAR_FRESNEL: {
+        auto r = std::make_shared<SpecularFresnel>();
+        r->index = f[0];
+        m = r;
+        break;
+    }
+    case ORC_MAT_MF_NORMALMAP:
+        if (base < 0 || base >= (int)s->materials.size()) return -1;
+        m = std::make_shared<MicrofacetNormalMapping>(s->materials[base]);
+        break;
+    default: return -1;
+    }
+    if (normalmap >= 0) m->normalmap = s->textures[normalmap];
+    s->materials.push_back(m);
+    return (int)s->materials.size() - 1;
+}
+
+int xref_add_object(void* p, int mesh, int material, const float* mat, const float* matInv) {
+    RefScene* s = (RefScene*)p;
+    if (mesh < 0 || mesh >= (int)s->meshes.size() || material < 0 || material >= (int)s->materials.size()) return -1;
+    s->scene.addObject(std::make_shared<Object>(s->meshes[mesh], s->materials[material], toTransform(mat, matInv)));
+    return 0;
+}
+
+int xref_set_camera(void* p, const float* c2w, const float* c2wInv, float fov, float aspect) {
+    RefScene* s = (RefScene*)p;
+    s->scene.camera = std::make_shared<PinholeCamera>(toTransform(c2w, c2wInv), fov, aspect);
+    return 0;
+}
+
+int xref_set_sky(void* p, int type, const float* rgb, int tex) {
+    RefScene* s = (RefScene*)p;
+    switch (type) {
+    case ORC_SKY_NONE: s->scene.skySphere = nullptr; return 0;
+    case ORC_SKY_UNIFORM: s->scene.skySphere = std::make_shared<SkySphereUniform>(Vector3f(rgb[0], rgb[1], rgb[2])); return 0;
+    case ORC_SKY_PROBE:
+        if (tex < 0 || tex >= (int)s->textures.size()) return -1;
+        s->scene.skySphere = std::make_shared<SkySphereFromImage>(s->textureNames[tex]);
+        return 0;
+    case ORC_SKY_LATLONG:
+        if (tex < 0 || tex >= (int)s->textures.size()) return -1;
+        s->scene.skySphere = std::make_shared<SkySphereLatLong>(s->textures[tex]);
+        return 0;
+    }
+    return -1;
+}
+
+int xref_build(void* p) {
+    RefScene* s = (RefScene*)p;
+    s->scene.buildAccelerationStructure();
+    s->built = true;
+    return 0;
+}
+
+// Per-(pixel, sample) PCG render. Only the reference's defaults are available
+// (its Russian-roulette constants are private, PathTracer.h:253-257, and it has
+// no depth limit), so other parameter values are rejected.
+int xref_render_pcg(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                    int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                    int nthreads) {
+    RefScene* s = (RefScene*)p;
+    if (!s->built || !s->scene.camera) return -1;
+    if (max_depth != 0 || rr_start != 5 || rr_prob != 0.9f) return -2;
+    RenderTarget<Vector3f> target(W, H);
+    StandardPathTracer standard;
+    NaivePathTracer naive;
+    const PathTracer& pt = integrator == ORC_INTEGRATOR_NAIVE ? (const PathTracer&)naive : (const PathTracer&)standard;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = y0; y < y1; ++y) {
+        PcgSampler sampler;
+        RenderTargetTile<Vector3f> tile;
+        tile.image = &target;
+        tile.sampler = std::shared_ptr<Sampler>(&sampler, [](Sampler*) {});
+        for (int x = x0; x < x1; ++x) {
+            uint32_t pixel = (uint32_t)(x + y * W);
+            tile.offset = Vector2i((x / RenderTargetTile<Vector3f>::Width) * RenderTargetTile<Vector3f>::Width,
+                                   (y / RenderTargetTile<Vector3f>::Height) * RenderTargetTile<Vector3f>::Height);
+            Vector2i local(x - tile.offset.x, y - tile.offset.y);
+            Vector3f sum;
+            for (uint32_t k = 0; k < spp_count; ++k) {
+                sampler.seedPath(pixel, spp_begin + k, seed);
+                Vector2f pFilm = tile.GenerateFilmPosition(local, true);
+                Ray ray = s->scene.camera->generateRay(pFilm, sampler);
+                sum += pt.eval(s->scene, sampler, ray).color;
+            }
+            float* px = film + 3 * (size_t)pixel;
+            px[0] += sum.x; px[1] += sum.y; px[2] += sum.z;
+        }
+    }
+    return 0;
+}
+
+// The reference's stock render call exactly as the sandboxes drive it
+// (SimplePathTracer/Main.cpp:134-138): RenderTarget::render over 16x16 tiles,
+// one Mersenne-Twister sampler per tile, OpenMP over tiles. Returns the wall
+// time in seconds; the film receives the radiance sums.
+double xref_render_stock(void* p, int W, int H, int spp, int integrator, float* film, int nthreads) {
+    RefScene* s = (RefScene*)p;
+    if (!s->built || !s->scene.camera) return -1.0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    SimpleRenderTarget target(W, H);
+    target.clear();
+    StandardPathTracer standard;
+    NaivePathTracer naive;
+    const PathTracer& pt = integrator == ORC_INTEGRATOR_NAIVE ? (const PathTracer&)naive : (const PathTracer&)standard;
+    auto t0 = std::chrono::steady_clock::now();
+    target.render(s->scene, spp, [&](const Vector2f& pFilm, Sampler& sampler, Vector3f& color) {
+        auto ray = s->scene.camera->generateRay(pFilm, sampler);
+        color += pt.eval(s->scene, sampler, ray).color;
+    });
+    auto t1 = std::chrono::steady_clock::now();
+    for (int i = 0; i < W * H; ++i) {
+        film[3 * i] = target.data[i].x;
+        film[3 * i + 1] = target.data[i].y;
+        film[3 * i + 2] = target.data[i].z;
+    }
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// vMF mixture (VonMisesFisherDistribution.h) for L = 8 lobes: the fit
+// (approximateBySEM, :68-160), the mixture pdf (eval, :60-66) and sampling
+// (sample, :162-201). Encoded parameters follow encode() (:37-45).
+int xref_vmf8_fit(const float* samples, int n, uint32_t seed, float* encoded) {
+    std::vector<Vector3f> v(n);
+    for (int i = 0; i < n; ++i) v[i] = Vector3f(samples[3 * i], samples[3 * i + 1], samples[3 * i + 2]);
+    Sampler sampler((int)seed);
+    auto vmf = VonMisesFisherDistribution<8>::approximateBySEM(v, sampler);
+    vmf.encode(encoded);
+    return 0;
+}
+int xref_vmf8_eval(const float* encoded, int n, const float* dirs, float* pdf) {
+    VonMisesFisherDistribution<8> vmf;
+    vmf.decode(encoded);
+    for (int i = 0; i < n; ++i) pdf[i] = vmf.eval(Vector3f(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+    return 0;
+}
+int xref_vmf8_sample_pcg(const float* encoded, int n, uint32_t seed, float* dirs) {
+    VonMisesFisherDistribution<8> vmf;
+    vmf.decode(encoded);
+    PcgSampler sampler;
+    for (int i = 0; i < n; ++i) {
+        sampler.seedPath((uint32_t)i, 0, seed);
+        Vector3f d = vmf.sample(sampler);
+        dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    }
+    return 0;
+}
+}  // extern "C"

@@ -1,0 +1,91 @@
+"""The oracle (oracle/xgb_cpu.cpp) against the reference's own code.
+
+Golden films in tests/golden were rendered by the reference headers
+(tests/golden/make_golden.py); the live comparisons run the reference through
+oracle/_ref when its staged sources are present. The bar is bit-exact: the
+oracle restates the reference's arithmetic in the same order.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.bindings import CpuChecker, load_scene
+from xitils_gb300 import scenes
+from xitils_gb300.scene import NAIVE, IntegratorParams
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_films.npz")
+
+
+def _ref_available():
+    try:
+        CpuChecker("reference")
+        return True
+    except Exception:
+        return False
+
+
+REF = _ref_available()
+needs_ref = pytest.mark.skipif(not REF, reason="reference checker not staged")
+
+
+@pytest.mark.parametrize("name,make,params", [
+    ("cornell_48x48x4", lambda: scenes.cornell(48, 48, 4), IntegratorParams()),
+    ("cornell_naive_32x32x4", lambda: scenes.cornell(32, 32, 4), IntegratorParams(integrator=NAIVE)),
+    ("simple_path_tracer_48x48x4", lambda: scenes.simple_path_tracer_scene(48, 48, 4), IntegratorParams()),
+    ("terrain_g65_40x40x2", lambda: scenes.terrain(grid=65, width=40, height=40, spp=2, env_size=(128, 64)),
+     IntegratorParams()),
+])
+def test_oracle_matches_golden(name, make, params):
+    golden = np.load(GOLDEN)[name]
+    desc = make()
+    film = load_scene(desc, "port").render_pcg(desc, params=params)
+    assert film.shape == golden.shape
+    assert np.array_equal(film, golden)
+
+
+@needs_ref
+@pytest.mark.parametrize("sky", ["none", "uniform", "probe", "latlong"])
+def test_oracle_matches_reference_material_zoo(sky):
+    desc = scenes.material_zoo(40, 40, 4, sky=sky)
+    a = load_scene(desc, "port").render_pcg(desc, params=IntegratorParams())
+    b = load_scene(desc, "reference").render_pcg(desc, params=IntegratorParams())
+    assert np.array_equal(a, b)
+
+
+@needs_ref
+def test_oracle_matches_reference_pixel_rect_and_sample_range():
+    desc = scenes.cornell(40, 40, 6)
+    P = IntegratorParams(seed=11)
+    port, ref = load_scene(desc, "port"), load_scene(desc, "reference")
+    a = port.render_pcg(desc, spp_begin=3, spp_count=3, rect=(5, 7, 33, 29), params=P)
+    b = ref.render_pcg(desc, spp_begin=3, spp_count=3, rect=(5, 7, 33, 29), params=P)
+    assert np.array_equal(a, b)
+    assert a[:7].sum() == 0 and a[:, :5].sum() == 0  # outside the rectangle stays empty
+
+
+def test_oracle_sample_ranges_add_up():
+    """Counter-based streams: rendering samples [0,2) and [2,4) separately sums to [0,4)."""
+    desc = scenes.cornell(24, 24, 4)
+    chk = load_scene(desc, "port")
+    P = IntegratorParams(max_depth=8, rr_start=3)
+    full = chk.render_pcg(desc, 0, 4, params=P)
+    part = chk.render_pcg(desc, 0, 2, params=P) + chk.render_pcg(desc, 2, 2, params=P)
+    np.testing.assert_allclose(part, full, rtol=1e-5, atol=1e-5)
+
+
+def test_oracle_depth_limit_and_rr_params():
+    """max_depth / rr_start change the estimate of a closed box only through
+    truncation: a deeper limit never loses energy on average."""
+    desc = scenes.cornell(32, 32, 16)
+    chk = load_scene(desc, "port")
+    shallow = chk.render_pcg(desc, params=IntegratorParams(max_depth=2, rr_start=100)).mean()
+    deep = chk.render_pcg(desc, params=IntegratorParams(max_depth=8, rr_start=100)).mean()
+    assert 0 < shallow < deep
+
+
+@needs_ref
+def test_reference_rejects_non_default_params():
+    desc = scenes.cornell(8, 8, 1)
+    with pytest.raises(RuntimeError):
+        load_scene(desc, "reference").render_pcg(desc, params=IntegratorParams(max_depth=8))

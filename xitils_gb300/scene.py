@@ -1,0 +1,155 @@
+"""Backend-neutral scene description.
+
+A ``SceneDesc`` records what a Xitils program passes to the reference's
+construction API -- ``TriangleMesh::setGeometry`` (TriangleMesh.h:151-161),
+``Object(shape, material, transform)`` (Object.h:32-34), the material
+constructors (Material.h), ``Scene::addObject`` (Scene.h:17-22), the camera and
+the sky -- as plain numpy arrays, and replays it into any backend that exposes
+the same calls: the GPU library (``xitils_gb300.api``) or, in tests, the CPU
+checkers.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from .transform import Transform
+
+# Material kinds (same numbering as the C ABI's xgb_material_kind).
+DIFFUSE, METAL, GLOSSY, GLOSSY_HIGHLIGHT, GLOSSY_CLAMPED, EMISSION = 0, 1, 2, 3, 4, 5
+SPECULAR_REFLECTION, SPECULAR_REFRACTION, SPECULAR_FRESNEL, MF_NORMALMAP = 6, 7, 8, 9
+# Sky kinds.
+SKY_NONE, SKY_UNIFORM, SKY_PROBE, SKY_LATLONG = 0, 1, 2, 3
+# Integrators.
+STANDARD, NAIVE = 0, 1
+
+
+@dataclass
+class TextureDesc:
+    rgb: np.ndarray  # float32 [h, w, 3]
+    clamp: bool = True
+    filter: bool = True
+
+
+@dataclass
+class MeshDesc:
+    pos: np.ndarray  # float32 [nV, 3]
+    idx: np.ndarray  # int32 [nIdx]
+    uv: Optional[np.ndarray] = None
+    nrm: Optional[np.ndarray] = None
+    tan: Optional[np.ndarray] = None
+    bit: Optional[np.ndarray] = None
+
+    @property
+    def n_tris(self) -> int:
+        return int(self.idx.size // 3)
+
+
+@dataclass
+class MaterialDesc:
+    kind: int
+    f: list
+    base: int = -1
+    tex: int = -1
+    normalmap: int = -1
+
+
+@dataclass
+class ObjectDesc:
+    mesh: int
+    material: int
+    transform: Transform
+
+
+@dataclass
+class IntegratorParams:
+    """Integrator settings. Reference defaults: no depth limit, Russian roulette
+    when pathLength > 5 with survival 0.9 (PathTracer.h:253-257)."""
+    integrator: int = STANDARD
+    max_depth: int = 0
+    rr_start: int = 5
+    rr_prob: float = 0.9
+    seed: int = 0
+
+
+@dataclass
+class SceneDesc:
+    name: str = "scene"
+    textures: list = field(default_factory=list)
+    meshes: list = field(default_factory=list)
+    materials: list = field(default_factory=list)
+    objects: list = field(default_factory=list)
+    camera: tuple = None  # (Transform, fov_radians, aspect)
+    sky: tuple = (SKY_NONE, None, -1)
+    width: int = 64
+    height: int = 64
+    spp: int = 1
+    params: IntegratorParams = field(default_factory=IntegratorParams)
+
+    # -- construction -----------------------------------------------------
+    def add_texture(self, rgb: np.ndarray, clamp: bool = True, filter: bool = True) -> int:
+        rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+        assert rgb.ndim == 3 and rgb.shape[2] == 3
+        self.textures.append(TextureDesc(rgb, clamp, filter))
+        return len(self.textures) - 1
+
+    def add_mesh(self, pos, idx, uv=None, nrm=None, tan=None, bit=None) -> int:
+        c = lambda a, k: None if a is None else np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, k))
+        m = MeshDesc(c(pos, 3), np.ascontiguousarray(np.asarray(idx, dtype=np.int32).reshape(-1)),
+                     c(uv, 2), c(nrm, 3), c(tan, 3), c(bit, 3))
+        self.meshes.append(m)
+        return len(self.meshes) - 1
+
+    def add_material(self, kind: int, f=(), base: int = -1, tex: int = -1, normalmap: int = -1) -> int:
+        self.materials.append(MaterialDesc(kind, [float(x) for x in f], base, tex, normalmap))
+        return len(self.materials) - 1
+
+    def diffuse(self, albedo, tex: int = -1, normalmap: int = -1) -> int:
+        return self.add_material(DIFFUSE, albedo, tex=tex, normalmap=normalmap)
+
+    def metal(self, roughness: float, f0, rough_tex: int = -1, normalmap: int = -1) -> int:
+        return self.add_material(METAL, [roughness, *f0], tex=rough_tex, normalmap=normalmap)
+
+    def emission(self, power) -> int:
+        return self.add_material(EMISSION, power)
+
+    def add_object(self, mesh: int, material: int, transform: Optional[Transform] = None) -> int:
+        self.objects.append(ObjectDesc(mesh, material, transform or Transform.identity()))
+        return len(self.objects) - 1
+
+    def set_camera(self, c2w: Transform, fov: float, aspect: float) -> None:
+        self.camera = (c2w, float(fov), float(aspect))
+
+    def set_sky(self, kind: int, rgb=None, tex: int = -1) -> None:
+        self.sky = (kind, None if rgb is None else [float(x) for x in rgb], tex)
+
+    # -- facts ---------------------------------------------------------------
+    @property
+    def n_tris(self) -> int:
+        return sum(self.meshes[o.mesh].n_tris for o in self.objects)
+
+    @property
+    def n_paths(self) -> int:
+        return self.width * self.height * self.spp
+
+    # -- replay ----------------------------------------------------------------
+    def emit(self, backend):
+        """Replay into a backend exposing add_texture / add_mesh / add_material /
+        add_object / set_camera / set_sky / build (see xitils_gb300.api.Scene and
+        the CPU checker bindings)."""
+        for t in self.textures:
+            backend.add_texture(t.rgb, t.clamp, t.filter)
+        for m in self.meshes:
+            backend.add_mesh(m.pos, m.idx, m.uv, m.nrm, m.tan, m.bit)
+        for mt in self.materials:
+            backend.add_material(mt.kind, mt.f, mt.base, mt.tex, mt.normalmap)
+        for o in self.objects:
+            backend.add_object(o.mesh, o.material, o.transform.mat, o.transform.matInv)
+        c2w, fov, aspect = self.camera
+        backend.set_camera(c2w.mat, c2w.matInv, fov, aspect)
+        kind, rgb, tex = self.sky
+        backend.set_sky(kind, rgb, tex)
+        backend.build()
+        return backend

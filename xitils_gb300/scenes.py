@@ -1,0 +1,244 @@
+"""Seeded synthetic scenes for the benchmark workloads.
+
+No external asset is used: every mesh, texture and environment map is generated
+here from a fixed seed, with the sizes and value distributions of the workloads
+(Cornell box, fBm heightfield terrain, batched random scenes, occluded-light
+room, microfacet-normal-mapped terrain). Scenes are built through the same
+construction calls a Xitils program makes (``SceneDesc`` records them).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .scene import (DIFFUSE, EMISSION, METAL, MF_NORMALMAP, SKY_LATLONG, SKY_UNIFORM, IntegratorParams, SceneDesc)
+from .transform import Transform, transformTRS, translate
+
+F = np.float32
+
+
+# ------------------------------------------------------------------ helpers --
+def _normalize32(v):
+    v = np.asarray(v, dtype=F)
+    l2 = F(F(v[0] * v[0] + v[1] * v[1]) + F(v[2] * v[2]))
+    inv = F(F(1) / F(np.sqrt(l2)))
+    return (v * inv).astype(F)
+
+
+def _cross64(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]], dtype=F)
+
+
+def look_at(pos, look, up) -> Transform:
+    """lookAt (Transform.h:344-368): columns right / newUp / dir, translation pos;
+    like the reference, the stored inverse is the transpose."""
+    pos = np.asarray(pos, dtype=F)
+    d = _normalize32(np.asarray(look, dtype=F) - pos)
+    right = _normalize32(_cross64(_normalize32(up), d))
+    new_up = _cross64(d, right)
+    m = np.zeros((4, 4), dtype=F)
+    m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = right, new_up, d, pos
+    m[3, 3] = 1
+    return Transform.from_matrix(m)
+
+
+def unit_cube_mesh():
+    """The reference's Cube (TriangleMesh.h:369-397): corners at +-0.5."""
+    pos = np.array([[-0.5 if i & 1 else 0.5, -0.5 if i & 2 else 0.5, -0.5 if i & 4 else 0.5] for i in range(8)], dtype=F)
+    idx = np.array([0, 1, 2, 1, 3, 2, 2, 3, 6, 3, 7, 6, 0, 4, 1, 4, 5, 1, 0, 2, 6, 0, 6, 4,
+                    1, 5, 3, 5, 7, 3, 4, 6, 5, 6, 7, 5], dtype=np.int32)
+    return pos, idx
+
+
+def quad(p0, p1, p2, p3):
+    """Two triangles (p0,p1,p2), (p0,p2,p3); geometric normal = cross(p1-p0, p2-p0)."""
+    return np.array([p0, p1, p2, p3], dtype=F), np.array([0, 1, 2, 0, 2, 3], dtype=np.int32)
+
+
+# ---------------------------------------------------------------- Cornell box --
+def cornell(width: int = 512, height: int = 512, spp: int = 16, max_depth: int = 8, rr_start: int = 3,
+            seed: int = 0) -> SceneDesc:
+    """Cornell box: unit box [0,1]^3 of 5 quads (Lambert 0.75 grey, left wall
+    (0.63,0.065,0.05), right wall (0.14,0.45,0.09)), a 0.3x0.6x0.3 box rotated 15
+    degrees and a 0.3x0.3x0.3 box rotated -18 degrees, a 0.25x0.25 light quad at
+    y=0.999 facing -y with radiance (17,12,4). 36 triangles."""
+    s = SceneDesc(name="cornell", width=width, height=height, spp=spp,
+                  params=IntegratorParams(max_depth=max_depth, rr_start=rr_start, rr_prob=0.9, seed=seed))
+    grey = s.diffuse([0.75, 0.75, 0.75])
+    red = s.diffuse([0.63, 0.065, 0.05])
+    green = s.diffuse([0.14, 0.45, 0.09])
+    light = s.emission([17.0, 12.0, 4.0])
+    walls = [
+        (quad([0, 0, 0], [1, 0, 0], [1, 0, 1], [0, 0, 1]), grey),    # floor
+        (quad([0, 1, 0], [0, 1, 1], [1, 1, 1], [1, 1, 0]), grey),    # ceiling
+        (quad([0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]), grey),    # back
+        (quad([0, 0, 0], [0, 0, 1], [0, 1, 1], [0, 1, 0]), red),     # left (x = 0)
+        (quad([1, 0, 0], [1, 1, 0], [1, 1, 1], [1, 0, 1]), green),   # right (x = 1)
+    ]
+    for (pos, idx), mat in walls:
+        s.add_object(s.add_mesh(pos, idx), mat)
+    lo, hi, y = 0.375, 0.625, 0.999
+    pos, idx = quad([lo, y, lo], [hi, y, lo], [hi, y, hi], [lo, y, hi])  # normal -y
+    s.add_object(s.add_mesh(pos, idx), light)
+    cpos, cidx = unit_cube_mesh()
+    cube = s.add_mesh(cpos, cidx)
+    s.add_object(cube, grey, transformTRS((0.33, 0.3, 0.62), (0, 15, 0), (0.3, 0.6, 0.3)))
+    s.add_object(cube, grey, transformTRS((0.67, 0.15, 0.33), (0, -18, 0), (0.3, 0.3, 0.3)))
+    s.set_camera(translate(0.5, 0.5, -1.3), 40.0 * math.pi / 180.0, height / width)
+    return s
+
+
+# ------------------------------------------------------------------ terrain --
+def fbm_heights(n: int, seed: int, octaves: int = 6, amplitude: float = 0.15, lacunarity: float = 2.0,
+                gain: float = 0.5, base_cells: int = 4) -> np.ndarray:
+    """Value-noise fBm on an n x n vertex grid over [0,1]^2 (float32)."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, n, dtype=np.float64)
+    h = np.zeros((n, n), dtype=np.float64)
+    amp, cells, norm = 1.0, base_cells, 0.0
+    for _ in range(octaves):
+        lattice = rng.random((cells + 2, cells + 2))
+        g = x * cells
+        i0 = np.floor(g).astype(np.int64)
+        t = g - i0
+        t = t * t * (3 - 2 * t)
+        i1 = i0 + 1
+        a = lattice[np.ix_(i0, i0)]
+        b = lattice[np.ix_(i0, i1)]
+        c = lattice[np.ix_(i1, i0)]
+        d = lattice[np.ix_(i1, i1)]
+        tz, tx = t[:, None], t[None, :]
+        h += amp * ((a * (1 - tx) + b * tx) * (1 - tz) + (c * (1 - tx) + d * tx) * tz)
+        norm += amp
+        amp *= gain
+        cells = int(cells * lacunarity)
+    return (amplitude * h / norm).astype(F)
+
+
+def heightfield_mesh(heights: np.ndarray, extent: float = 1.0):
+    n = heights.shape[0]
+    g = np.linspace(0.0, extent, n, dtype=F)
+    xx, zz = np.meshgrid(g, g)
+    pos = np.stack([xx, heights, zz], axis=-1).reshape(-1, 3).astype(F)
+    u = np.linspace(0.0, 1.0, n, dtype=F)
+    uu, vv = np.meshgrid(u, u)
+    uv = np.stack([uu, vv], axis=-1).reshape(-1, 2).astype(F)
+    i = np.arange(n - 1, dtype=np.int64)
+    r, c = np.meshgrid(i, i, indexing="ij")
+    v00 = (r * n + c).ravel()
+    v01, v10, v11 = v00 + 1, v00 + n, v00 + n + 1
+    idx = np.stack([v00, v10, v11, v00, v11, v01], axis=-1).reshape(-1).astype(np.int32)
+    return pos, uv, idx
+
+
+def latlong_sky(width: int = 1024, height: int = 512, sun_dir=(0.45, 0.55, -0.35), kappa: float = 2000.0,
+                peak: float = 5.0e4) -> np.ndarray:
+    """Procedural HDR lat-long map: sky gradient plus a sun lobe
+    peak * exp(kappa * (mu . w - 1)). Texel (i, j) looks along the direction with
+    u = atan2(x, -z) / 2pi + 1/2, v = acos(y) / pi (the lat-long lookup)."""
+    u = (np.arange(width) + 0.5) / width
+    v = (np.arange(height) + 0.5) / height
+    phi = (u - 0.5) * 2 * np.pi
+    theta = v * np.pi
+    st, ct = np.sin(theta)[:, None], np.cos(theta)[:, None]
+    x = st * np.sin(phi)[None, :]
+    y = np.broadcast_to(ct, (height, width))
+    z = -st * np.cos(phi)[None, :]
+    up = np.clip(y, 0.0, 1.0)[..., None]
+    horizon = np.array([0.95, 0.9, 0.85])
+    zenith = np.array([0.25, 0.45, 0.95])
+    ground = np.array([0.18, 0.15, 0.12])
+    sky = np.where(y[..., None] >= 0.0, horizon * (1 - np.sqrt(up)) + zenith * np.sqrt(up), ground)
+    mu = np.asarray(sun_dir, dtype=np.float64)
+    mu = mu / np.linalg.norm(mu)
+    cosw = x * mu[0] + y * mu[1] + z * mu[2]
+    sun = peak * np.exp(kappa * (cosw - 1.0))
+    rgb = sky + sun[..., None] * np.array([1.0, 0.92, 0.8])
+    return rgb.astype(F)
+
+
+def terrain(grid: int = 1024, width: int = 1024, height: int = 1024, spp: int = 64, max_depth: int = 10,
+            seed: int = 7, env_size=(1024, 512)) -> SceneDesc:
+    """Displacement-heightfield terrain: grid x grid vertices (2*(grid-1)^2
+    triangles) with seeded 6-octave fBm heights (amplitude 0.15, lacunarity 2,
+    gain 0.5), a GGX conductor whose roughness is uniform per texel in
+    [0.05, 0.5], lit by a procedural lat-long HDR environment (sky gradient plus
+    a kappa=2000 sun lobe of peak radiance 5e4)."""
+    s = SceneDesc(name="terrain", width=width, height=height, spp=spp,
+                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed))
+    h = fbm_heights(grid, seed)
+    pos, uv, idx = heightfield_mesh(h)
+    rng = np.random.default_rng(seed + 1)
+    cells = max(grid - 1, 1)
+    rough = rng.uniform(0.05, 0.5, size=(cells, cells)).astype(F)
+    rough_tex = s.add_texture(np.repeat(rough[..., None], 3, axis=2), clamp=True, filter=False)
+    env = s.add_texture(latlong_sky(*env_size), clamp=True, filter=True)
+    mat = s.metal(0.3, [0.95, 0.64, 0.54], rough_tex=rough_tex)
+    s.add_object(s.add_mesh(pos, idx, uv=uv), mat)
+    s.set_sky(SKY_LATLONG, tex=env)
+    s.set_camera(look_at((0.5, 0.42, -0.25), (0.5, 0.02, 0.55), (0, 1, 0)), 50.0 * math.pi / 180.0, height / width)
+    return s
+
+
+def simple_path_tracer_scene(width: int = 128, height: int = 128, spp: int = 4) -> SceneDesc:
+    """The reference's SimplePathTracer sandbox scene (Sandbox/SimplePathTracer/
+    Main.cpp:66-114) with the Cinder teapot (unavailable) replaced by a Metal(0.3)
+    unit cube scaled 1.2 and rotated 15 degrees; reference integrator defaults."""
+    s = SceneDesc(name="simple_path_tracer", width=width, height=height, spp=spp, params=IntegratorParams())
+    white = s.diffuse([0.8, 0.8, 0.8])
+    red = s.diffuse([0.8, 0.1, 0.1])
+    green = s.diffuse([0.1, 0.8, 0.1])
+    light = s.emission([8.0, 8.0, 7.6])
+    metal = s.metal(0.3, [0.9, 0.9, 0.9])
+    cpos, cidx = unit_cube_mesh()
+    cube = s.add_mesh(cpos, cidx)
+    ppos = np.array([[-0.5 if i & 1 else 0.5, -0.5 if i & 2 else 0.5, 0.0] for i in range(4)], dtype=F)
+    plane = s.add_mesh(ppos, np.array([0, 2, 1, 1, 2, 3], dtype=np.int32))  # TriangleMesh.h:399-423
+    s.add_object(cube, white, transformTRS((0, 0, 0), (0, 0, 0), (4, 0.01, 4)))
+    s.add_object(cube, green, transformTRS((2, 2, 0), (0, 0, 0), (0.01, 4, 4)))
+    s.add_object(cube, red, transformTRS((-2, 2, 0), (0, 0, 0), (0.01, 4, 4)))
+    s.add_object(cube, white, transformTRS((0, 2, 2), (0, 0, 0), (4, 4, 0.01)))
+    s.add_object(cube, white, transformTRS((0, 4, 0), (0, 0, 0), (4, 0.01, 4)))
+    s.add_object(plane, light, transformTRS((0, 4.0 - 0.01, 0), (-90, 0, 0), (2.0, 2.0, 2.0)))
+    s.add_object(cube, metal, transformTRS((0, 0.6, 0), (0, 15, 0), (1.2, 1.2, 1.2)))
+    s.set_camera(translate(0, 2.0, -5), 60.0 * math.pi / 180.0, height / width)
+    return s
+
+
+def material_zoo(width: int = 64, height: int = 64, spp: int = 8, sky: str = "none", seed: int = 3) -> SceneDesc:
+    """The SimplePathTracer room plus tangent-space cubes covering every material
+    kind: Glossy, GlossyClamped under MicrofacetNormalMapping with a normal map,
+    GlossyWithHighLight, SpecularReflection, SpecularFresnel. ``sky`` is one of
+    none / uniform / probe / latlong."""
+    from .scene import (GLOSSY, GLOSSY_CLAMPED, GLOSSY_HIGHLIGHT, SKY_PROBE, SPECULAR_FRESNEL,
+                        SPECULAR_REFLECTION, MaterialDesc)
+    s = simple_path_tracer_scene(width, height, spp)
+    s.name = f"material_zoo_{sky}"
+    rng = np.random.default_rng(seed)
+    nm = s.add_texture(np.clip(rng.normal([0.5, 0.5, 1.0], [0.15, 0.15, 0.05], (32, 32, 3)), 0, 1).astype(F))
+    s.materials[4] = MaterialDesc(GLOSSY, [0.7, 0.6, 0.5, 40.0])
+    base = s.add_material(GLOSSY_CLAMPED, [0.8, 0.8, 0.8, 30.0])
+    mf = s.add_material(MF_NORMALMAP, [], base=base, normalmap=nm)
+    gh = s.add_material(GLOSSY_HIGHLIGHT, [0.5, 0.5, 0.5, 1, 1, 1, 5.0, 200.0, 0.3])
+    spec = s.add_material(SPECULAR_REFLECTION, [])
+    fres = s.add_material(SPECULAR_FRESNEL, [1.5])
+    cpos, cidx = unit_cube_mesh()
+    uv = cpos[:, :2] + 0.5
+    nrm = cpos / np.linalg.norm(cpos, axis=1, keepdims=True)
+    tan = np.tile([1.0, 0.0, 0.0], (8, 1))
+    bit = np.tile([0.0, 1.0, 0.0], (8, 1))
+    cm = s.add_mesh(cpos, cidx, uv=uv, nrm=nrm, tan=tan, bit=bit)
+    s.add_object(cm, mf, transformTRS((-1.0, 0.7, -0.5), (10, 30, 0), (0.8, 0.8, 0.8)))
+    s.add_object(cm, gh, transformTRS((1.2, 0.5, -0.8), (0, -20, 5), (0.6, 0.6, 0.6)))
+    s.add_object(cm, spec, transformTRS((1.0, 1.6, 0.5), (0, 40, 0), (0.5, 0.5, 0.5)))
+    s.add_object(cm, fres, transformTRS((-1.2, 1.8, 0.2), (20, 10, 0), (0.5, 0.5, 0.5)))
+    if sky == "uniform":
+        s.set_sky(SKY_UNIFORM, rgb=[0.2, 0.3, 0.4])
+    elif sky == "probe":
+        s.set_sky(SKY_PROBE, tex=s.add_texture(rng.random((64, 64, 3)).astype(F)))
+    elif sky == "latlong":
+        s.set_sky(SKY_LATLONG, tex=s.add_texture(latlong_sky(128, 64)))
+    return s
