@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GPU path tracer (Mpaths/s) on the terrain workload.
+
+Workload (one step = one render call of the whole film):
+  fBm heightfield terrain, 1024 x 1024 vertex grid (2,093,058 triangles), GGX
+  conductor with per-texel roughness U[0.05, 0.5], procedural 1024 x 512 lat-long
+  HDR environment (sky gradient + kappa=2000 sun of peak 5e4), 1024 x 1024 film,
+  64 samples per pixel, max depth 10, plain NEE + BSDF MIS path tracer.
+  Inputs are seeded synthetic data; the BVH + triangles (~0.3 GB) exceed L2.
+
+Arms:
+  default           : libxgb.so through its C ABI (ctypes), device-timed with CUDA
+                      events on the render stream; e2e = the same call with the film
+                      downloaded to pinned host memory every step.
+  --impl reference  : the reference's own CPU path tracer (oracle/_ref: Xitils
+                      headers, RenderTarget::render with per-tile samplers, OpenMP on
+                      all host cores) on a bounded sample of the same scene.
+
+Multi-GPU (torchrun, N > 1): replicas -- every rank renders its own disjoint
+sample range of the same film (weak scaling, no data-path collective); the
+timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 1024 * 1024
+# Algorithmic bytes of one closest-hit ray in the extension kernel: ray origin +
+# direction read (2 x 16 B), hit record written (16 B + 4 B instance id).
+EXTEND_BYTES_PER_RAY = 52
+# BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
+NODE_BYTES, TRI_BYTES = 64, 48
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="xgb", choices=["xgb", "reference"])
+    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell"])
+    p.add_argument("--grid", type=int, default=1024)
+    p.add_argument("--res", type=int, default=None)
+    p.add_argument("--spp", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-res", type=int, default=1024)
+    p.add_argument("--cpu-sample-spp", type=int, default=4)
+    return p.parse_args()
+
+
+def make_workload(args):
+    from xitils_gb300 import scenes
+    if args.workload == "terrain":
+        res = args.res or 1024
+        spp = args.spp or 64
+        desc = scenes.terrain(grid=args.grid, width=res, height=res, spp=spp, max_depth=10)
+        label = (f"terrain {args.grid}x{args.grid} grid ({desc.n_tris} tris), {res}x{res} film, {spp} spp, "
+                 f"max depth 10, GGX per-texel roughness, lat-long env 1024x512")
+    else:
+        res = args.res or 512
+        spp = args.spp or 16
+        desc = scenes.cornell(res, res, spp)
+        label = f"cornell 36 tris, {res}x{res} film, {spp} spp, max depth 8, RR after depth 3"
+    return desc, label
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if "Active" in r[5 + k]:
+                        reasons.add(nm)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_sample(desc, res, spp, nthreads):
+    """The reference's own RenderTarget::render (oracle/_ref) on res x res x spp of the same scene."""
+    from oracle.bindings import CpuChecker
+    chk = CpuChecker("reference")
+    desc.emit(chk)
+    film, sec = chk.render_stock(res, res, spp, nthreads=nthreads)
+    return res * res * spp / sec / 1e6, sec
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    desc, label = make_workload(args)
+    res, spp = args.cpu_sample_res, 1
+    nthreads = os.cpu_count() or 1
+    try:
+        from oracle.bindings import CpuChecker
+        chk = CpuChecker("reference")
+    except Exception as e:
+        print(json.dumps({"impl": "reference", "unavailable": f"reference checker not built: {e}"}))
+        return 0
+    desc.emit(chk)
+    for _ in range(args.warmup):
+        chk.render_stock(res, res, spp, nthreads=nthreads)
+    times = []
+    for _ in range(args.steps):
+        _, sec = chk.render_stock(res, res, spp, nthreads=nthreads)
+        times.append(sec)
+    total = sum(times)
+    value = res * res * spp * args.steps / total / 1e6
+    out = {
+        "impl": "reference", "metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm terrain, procedural lat-long environment)",
+        "config": {"workload": label, "sample_per_step": f"{res}x{res} film x {spp} spp of the same scene and camera",
+                   "integrator": "reference StandardPathTracer defaults (no depth limit, RR after length 5)"},
+        "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": nthreads, "kind": "reference",
+                         "sample": f"{res}x{res}x{spp} per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_xgb(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from xitils_gb300 import api
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    desc, label = make_workload(args)
+    ctx = api.Context(local)
+    builder = api.load_scene(ctx, desc)
+    scene = builder.scene
+    W, H, spp = desc.width, desc.height, desc.spp
+    rt = api.RenderTarget(ctx, W, H)
+    stream = torch.cuda.Stream(device=local)
+    sptr = C.c_void_p(stream.cuda_stream)
+    params = desc.params
+    step_paths = W * H * spp
+    sample_base = rank * spp * (args.warmup + 2 * args.steps + 1)
+
+    def render(k):
+        rt.render(scene, spp, params, sample_base + k * spp, stream=sptr)
+
+    for k in range(args.warmup):
+        render(k)
+    torch.cuda.synchronize()
+    scene.set_profiling(True)
+    stats = []
+    with ClockSampler(local) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            render(args.warmup + k)
+            stats.append(scene.stats(stream=sptr))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    ms = e0.elapsed_time(e1)
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
+    if dist:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = world * step_paths * args.steps / (ms_max / 1e3) / 1e6
+    clk = clocks.summary()
+
+    # end to end through the C ABI: render call + film download to pinned host memory every step
+    scene.set_profiling(False)
+    host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+    host_np = host.numpy()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        render(args.warmup + args.steps + k)
+        rt.download(host_np, stream=sptr)
+    t1 = time.perf_counter()
+    e2e_s = torch.tensor([t1 - t0], dtype=torch.float64, device=f"cuda:{local}")
+    if dist:
+        dist.all_reduce(e2e_s, op=dist.ReduceOp.MAX)
+    e2e = world * step_paths * args.steps / float(e2e_s.item()) / 1e6
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    agg = {k: sum(s[k] for s in stats) for k in ("paths", "extension_rays", "shadow_rays", "iterations",
+                                                   "kernel_launches", "node_visits", "tri_tests")}
+    stage_ms = [sum(s["kernel_ms"][j] for s in stats) for j in range(5)]
+    stage_launch = [sum(s["stage_launches"][j] for s in stats) for j in range(5)]
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    ext_ms = stage_ms[2]
+    ext_launches = max(stage_launch[2], 1)
+    achieved = EXTEND_BYTES_PER_RAY * agg["extension_rays"] / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
+    roofline = {
+        "kernel": "k_extend (closest-hit traversal)",
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": hbm if hbm else 6800.0,
+        "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6.8 TB/s",
+        "unit": "GB/s",
+        "frac": (achieved / (hbm or 6800.0)) if achieved else None,
+        "traffic": None,
+        "algorithmic_bytes_per_launch": EXTEND_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
+        "avg_launch_ms": ext_ms / ext_launches,
+        "bvh_l2_gbs": ((NODE_BYTES * agg["node_visits"] + TRI_BYTES * agg["tri_tests"]) / (ext_ms / 1e3) / 1e9
+                       if ext_ms > 0 else None),
+        "nodes_per_ray": agg["node_visits"] / max(agg["extension_rays"], 1),
+        "tris_per_ray": agg["tri_tests"] / max(agg["extension_rays"], 1),
+    }
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            n = os.cpu_count() or 1
+            v, sec = cpu_reference_sample(desc, args.cpu_sample_res, args.cpu_sample_spp, n)
+            cpu = {"value": v, "unit": "Mpaths/s", "cores": n, "kind": "reference",
+                   "sample": f"{args.cpu_sample_res}x{args.cpu_sample_res} film x {args.cpu_sample_spp} spp of the "
+                             f"same scene ({sec:.1f} s), reference RenderTarget::render + StandardPathTracer"}
+        except Exception as e:
+            cpu = {"value": None, "unit": "Mpaths/s", "cores": os.cpu_count(), "kind": "reference",
+                   "sample": f"unavailable: {e}"}
+    total_rays = agg["extension_rays"] + agg["shadow_rays"]
+    out = {
+        "metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm terrain, procedural lat-long environment)",
+        "config": {"workload": label, "parallelism": f"replicas x{world} (disjoint sample ranges)",
+                   "l2": "inputs larger than L2 (BVH + triangles exceed 129 MB)",
+                   "queue_capacity": 1 << 21},
+        "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC),
+                "d2h_bytes_per_step": W * H * 12},
+        "gpu_launches": agg["kernel_launches"],
+        "mrays_per_s": total_rays * world / (ms_max / 1e3) / 1e6,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "stage_ms": {"plan": stage_ms[0], "generate": stage_ms[1], "extend": stage_ms[2], "shade": stage_ms[3],
+                     "shadow": stage_ms[4]},
+        "render_stats": agg,
+    }
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_xgb(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,191 @@
+/* xgb.h -- C ABI of the GB300 path tracer (libxgb.so).
+ *
+ * A drop-in for the render call of Xitils: the same scene-construction calls
+ * (meshes, materials, objects with transforms, camera, sky) go in, and a film
+ * of per-pixel radiance SUMS comes out, as RenderTarget::render leaves it.
+ * Plain C types only: handles are opaque, arrays are host pointers with sizes,
+ * CUDA streams travel as void* (cudaStream_t; NULL = the context's stream).
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the Xitils repository). Every call returns an xgb_status; on failure
+ * xgb_get_last_error() holds a message. Work is enqueued on the given stream;
+ * xgb_film_download() and xgb_render_stats() synchronise it.
+ */
+#ifndef XGB_H
+#define XGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    XGB_OK = 0,
+    XGB_INVALID_ARG = 1,     /* bad handle, size, index or parameter            */
+    XGB_OOM = 2,             /* device or host allocation failed                */
+    XGB_CUDA_ERROR = 3,      /* a CUDA runtime call failed                      */
+    XGB_QUEUE_OVERFLOW = 4,  /* a device work queue or traversal stack overflowed */
+    XGB_DEVICE_TIMEOUT = 5,  /* a bounded device wait gave up                   */
+    XGB_NOT_BUILT = 6,       /* scene used before xgb_scene_build               */
+    XGB_UNSUPPORTED = 7      /* feature not available in this build             */
+} xgb_status;
+
+typedef struct xgb_ctx xgb_ctx;
+typedef struct xgb_texture xgb_texture;
+typedef struct xgb_mesh xgb_mesh;
+typedef struct xgb_material xgb_material;
+typedef struct xgb_scene xgb_scene;
+typedef struct xgb_film xgb_film;
+
+/* ---------------------------------------------------------------- context */
+/* One context per GPU (and per host thread, or serialise calls on it). */
+xgb_status xgb_ctx_create(int device, xgb_ctx** out);
+xgb_status xgb_ctx_destroy(xgb_ctx* ctx);
+/* Last error message of this context ("" when none). Never NULL. */
+const char* xgb_get_last_error(const xgb_ctx* ctx);
+/* Library version string, e.g. "xgb 0.1 sm_103a". */
+const char* xgb_version(void);
+
+/* ---------------------------------------------------------------- texture */
+/* Texture(int w, int h) filled with float RGB texels, row y = 0 first
+ * (Include/Xitils/Texture.h:25-32, :77-103). wrap_clamp: 1 = clamp
+ * (Texture::warpClamp, default), 0 = wrap. filter: 1 = bilinear (default),
+ * 0 = nearest. channels: 3 (RGB) or 4 (RGBA, alpha ignored). The data is copied. */
+xgb_status xgb_texture_create(xgb_ctx* ctx, int width, int height, int channels, const float* texels,
+                              int wrap_clamp, int filter, xgb_texture** out);
+xgb_status xgb_texture_destroy(xgb_texture* tex);
+
+/* ------------------------------------------------------------------ meshes */
+/* TriangleMesh::setGeometry(vertexNum, positions, texCoords, normals, tangents,
+ * bitangents, indexNum, indices) (Include/Xitils/TriangleMesh.h:151-161).
+ * vec3_stride: byte stride of positions/normals/tangents/bitangents, 12 (packed
+ * float3) or 16 (xitils::Vector3f). uv_stride: 8 (packed float2) or 16
+ * (xitils::Vector2f). Optional arrays may be NULL; tangents need bitangents.
+ * Indices must lie in [0, vertex_count). All arrays are copied. */
+xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                           const float* normals, const float* tangents, const float* bitangents, int vec3_stride,
+                           int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out);
+xgb_status xgb_mesh_destroy(xgb_mesh* mesh);
+xgb_status xgb_mesh_triangle_count(const xgb_mesh* mesh, int* out);
+
+/* --------------------------------------------------------------- materials */
+/* Diffuse(albedo) (Include/Xitils/Material.h:50-86); albedo_tex optional (Diffuse::texture). */
+xgb_status xgb_material_diffuse(xgb_ctx* ctx, const float albedo[3], const xgb_texture* albedo_tex,
+                                xgb_material** out);
+/* Metal(roughness, f0): GGX conductor with VNDF sampling (Material.h:275-384).
+ * roughness_tex optional: per-hit roughness = red channel of a nearest lookup. */
+xgb_status xgb_material_metal(xgb_ctx* ctx, float roughness, const float f0[3], const xgb_texture* roughness_tex,
+                              xgb_material** out);
+/* Glossy(albedo, sharpness) (Material.h:88-132). */
+xgb_status xgb_material_glossy(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out);
+/* GlossyWithHighLight(albedo, highlight, sharpness, sharpnessHighLight, rate) (Material.h:134-175). */
+xgb_status xgb_material_glossy_highlight(xgb_ctx* ctx, const float albedo[3], const float highlight[3],
+                                         float sharpness, float sharpness_highlight, float rate, xgb_material** out);
+/* GlossyClamped(albedo, sharpness) (Sandbox/MicrofacetBasedNormalMapping/Main.cpp:34-84). */
+xgb_status xgb_material_glossy_clamped(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out);
+/* Emission(power) (Material.h:386-411): one-sided, emits where dot(wo, n) > 0. */
+xgb_status xgb_material_emission(xgb_ctx* ctx, const float power[3], xgb_material** out);
+/* SpecularReflection / SpecularRefraction(index) / SpecularFresnel(index) (Material.h:177-273). */
+xgb_status xgb_material_specular_reflection(xgb_ctx* ctx, xgb_material** out);
+xgb_status xgb_material_specular_refraction(xgb_ctx* ctx, float index, xgb_material** out);
+xgb_status xgb_material_specular_fresnel(xgb_ctx* ctx, float index, xgb_material** out);
+/* MicrofacetNormalMapping(base) (Sandbox/MicrofacetBasedNormalMapping/Main.cpp:86-340). */
+xgb_status xgb_material_mf_normalmap(xgb_ctx* ctx, const xgb_material* base, xgb_material** out);
+/* Material::normalmap (Material.h:13; applied in Object.h:58-68). NULL clears it. */
+xgb_status xgb_material_set_normalmap(xgb_material* mat, const xgb_texture* normalmap);
+xgb_status xgb_material_destroy(xgb_material* mat);
+
+/* ------------------------------------------------------------------- scene */
+xgb_status xgb_scene_create(xgb_ctx* ctx, xgb_scene** out);
+xgb_status xgb_scene_destroy(xgb_scene* scene);
+/* Scene::addObject(make_shared<Object>(mesh, material, Transform(mat, matInv)))
+ * (Include/Xitils/Scene.h:17-22, Object.h:32-34). mat / mat_inv: float[16]
+ * row-major m[r][c] (Matrix4x4). Emissive materials make the object a light,
+ * in insertion order. Meshes and materials must outlive the scene. */
+xgb_status xgb_scene_add_object(xgb_scene* scene, const xgb_mesh* mesh, const xgb_material* material,
+                                const float mat[16], const float mat_inv[16]);
+/* scene->camera = make_shared<PinholeCamera>(Transform(c2w, c2w_inv), fov, aspect)
+ * (Include/Xitils/Camera.h:32-55). fov in radians; aspect as the reference uses it
+ * (tan(fov/2 * aspect) for the vertical extent). */
+xgb_status xgb_scene_set_camera_pinhole(xgb_scene* scene, const float c2w[16], const float c2w_inv[16], float fov,
+                                        float aspect);
+/* scene->skySphere (Include/Xitils/SkySphere.h): none, SkySphereUniform(color),
+ * SkySphereFromImage (angular light probe), or a lat-long map
+ * (u = atan2(x, -z)/2pi + 1/2, v = acos(y)/pi). */
+xgb_status xgb_scene_set_sky_none(xgb_scene* scene);
+xgb_status xgb_scene_set_sky_uniform(xgb_scene* scene, const float rgb[3]);
+xgb_status xgb_scene_set_sky_probe(xgb_scene* scene, const xgb_texture* probe);
+xgb_status xgb_scene_set_sky_latlong(xgb_scene* scene, const xgb_texture* latlong);
+/* Scene::buildAccelerationStructure (Scene.h:24-28): uploads the scene and
+ * builds the bounding-volume hierarchies on the GPU. stream may be NULL. */
+xgb_status xgb_scene_build(xgb_scene* scene, void* stream);
+
+/* -------------------------------------------------------------------- film */
+/* RenderTarget<Vector3f>(width, height) (Include/Xitils/RenderTarget.h:13-23):
+ * per-pixel radiance sums in device memory, pixel (x, y) at x + y * width.
+ * fp64 = 1 accumulates in double (for very high sample counts). */
+xgb_status xgb_film_create(xgb_ctx* ctx, int width, int height, int fp64, xgb_film** out);
+xgb_status xgb_film_destroy(xgb_film* film);
+/* RenderTarget::clear (RenderTarget.h:29-31). */
+xgb_status xgb_film_clear(xgb_film* film, void* stream);
+/* Copies the sums to host memory as float RGB with the given pixel stride in
+ * bytes (12 = packed, 16 = xitils::Vector3f layout). Synchronises the stream. */
+xgb_status xgb_film_download(xgb_film* film, float* host, int pixel_stride_bytes, void* stream);
+/* Device address of the film (float4 or double4 per pixel, w unused). */
+xgb_status xgb_film_device_pointer(xgb_film* film, void** out, int* is_fp64);
+
+/* --------------------------------------------------------------- rendering */
+typedef enum { XGB_INTEGRATOR_STANDARD = 0, XGB_INTEGRATOR_NAIVE = 1 } xgb_integrator;
+
+typedef struct {
+    int integrator;   /* StandardPathTracer (NEE + BSDF sampling, power-heuristic MIS) or NaivePathTracer */
+    int max_depth;    /* 0 = unlimited (reference); else the loop stops when pathLength > max_depth */
+    int rr_start;     /* Russian roulette when pathLength > rr_start (reference: 5) */
+    float rr_prob;    /* survival probability (reference: 0.9) */
+    uint32_t seed;    /* PCG stream seed: stream(pixel, sample) = pcg32(splitmix64(seed<<32 ^ sample), pixel) */
+    int queue_capacity; /* paths in flight, 0 = automatic */
+} xgb_integrator_params;
+
+/* Fills the reference's defaults (PathTracer.h:253-257). */
+void xgb_integrator_params_default(xgb_integrator_params* p);
+
+/* RenderTarget::render(scene, spp, [&](pFilm, sampler, color) {
+ *     color += pathTracer.eval(scene, sampler, camera.generateRay(pFilm, sampler)).color; })
+ * (Include/Xitils/RenderTarget.h:109-127, PathTracer.h:117-251,
+ *  Sandbox/SimplePathTracer/Main.cpp:134-138). Adds the radiance of samples
+ * [spp_begin, spp_begin + spp_count) of every pixel to the film. Sample k of a
+ * pixel always draws from the same PCG stream, so disjoint sample ranges can be
+ * rendered separately (and on different GPUs) and summed. */
+xgb_status xgb_render(xgb_scene* scene, const xgb_integrator_params* params, xgb_film* film, uint32_t spp_begin,
+                      uint32_t spp_count, void* stream);
+
+typedef struct {
+    uint64_t paths;          /* camera paths completed */
+    uint64_t extension_rays; /* closest-hit rays traced */
+    uint64_t shadow_rays;    /* any-hit rays traced */
+    uint64_t iterations;     /* wavefront iterations that had work */
+    uint64_t kernel_launches;/* kernels launched by the call */
+    uint64_t node_visits;    /* BVH nodes visited by extension rays (profiling only) */
+    uint64_t tri_tests;      /* triangle tests of extension rays (profiling only) */
+    uint32_t error_flags;    /* device error bits: 1 traversal stack overflow */
+    uint32_t profiled;       /* 1 when the timings below were recorded */
+    /* summed device time per kernel stage, CUDA events on the render stream:
+       [0] plan, [1] generate, [2] extend (closest hit), [3] shade, [4] shadow (any hit) */
+    double kernel_ms[5];
+    uint64_t stage_launches[5];
+} xgb_render_stats;
+
+/* Counters of the last xgb_render on this scene. Synchronises the stream. */
+xgb_status xgb_render_stats_get(xgb_scene* scene, xgb_render_stats* out, void* stream);
+
+/* enable = 1: later xgb_render calls on this scene record CUDA events around
+ * every kernel on the render stream and count BVH work (for profiling; adds a
+ * few microseconds per wavefront iteration). */
+xgb_status xgb_scene_set_profiling(xgb_scene* scene, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XGB_H */

@@ -1,0 +1,108 @@
+"""GPU path (libxgb.so through the C ABI) against the oracle on the same
+scenes and the same per-(pixel, sample) PCG streams.
+
+Tolerance (floating point): image relMSE <= 1e-4 with eps = 1e-2, the bar the
+path tracer is held to. The shading arithmetic is unfused FP32 like the
+reference's; transcendental functions are CUDA's, so a path can still diverge
+where a decision sits within an ulp of its threshold -- rare enough that most
+pixels agree to ~1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle.bindings import load_scene as load_cpu, relmse
+from xitils_gb300 import scenes
+from xitils_gb300.scene import NAIVE, IntegratorParams
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import __graft_entry__ as g
+    g.build()
+    from xitils_gb300 import api
+    return api.Context(0)
+
+
+def _compare(ctx, desc, params=None, **kw):
+    from xitils_gb300 import api
+    P = params or desc.params
+    gpu = api.render_desc(ctx, desc, params=P, **kw)
+    cpu = load_cpu(desc, "port").render_pcg(desc, params=P, spp_begin=kw.get("spp_begin", 0),
+                                            spp_count=kw.get("spp_count"))
+    err = relmse(gpu, cpu)
+    close = np.mean(np.abs(gpu - cpu) <= 1e-3 * (np.abs(cpu) + 1e-2))
+    print(f"{desc.name}: relMSE {err:.3e}, pixels within 1e-3: {close:.4f}, means {gpu.mean():.5f} {cpu.mean():.5f}")
+    assert np.isfinite(gpu).all()
+    return gpu, cpu, err, close
+
+
+@pytest.mark.parametrize("make,params", [
+    (lambda: scenes.cornell(96, 96, 16), None),                                    # max depth 8, RR after 3
+    (lambda: scenes.cornell(80, 64, 8), IntegratorParams()),                       # reference defaults
+    (lambda: scenes.cornell(64, 64, 8), IntegratorParams(integrator=NAIVE)),
+    (lambda: scenes.simple_path_tracer_scene(96, 96, 8), None),
+])
+def test_cornell_family(ctx, make, params):
+    _, _, err, close = _compare(ctx, make(), params)
+    assert err <= TOL
+    assert close >= 0.98
+
+
+def test_terrain_ggx_latlong(ctx):
+    desc = scenes.terrain(grid=129, width=96, height=96, spp=8, env_size=(256, 128))
+    _, _, err, close = _compare(ctx, desc)
+    assert err <= TOL
+    assert close >= 0.98
+
+
+@pytest.mark.parametrize("sky", ["none", "uniform", "probe", "latlong"])
+def test_material_zoo(ctx, sky):
+    desc = scenes.material_zoo(64, 64, 8, sky=sky)
+    _, _, err, close = _compare(ctx, desc, IntegratorParams())
+    assert err <= TOL
+    assert close >= 0.95
+
+
+def test_sample_ranges_add_up_and_match_oracle(ctx):
+    from xitils_gb300 import api
+    desc = scenes.cornell(48, 48, 6)
+    b = api.load_scene(ctx, desc)
+    rt = api.RenderTarget(ctx, 48, 48)
+    rt.render(b.scene, 3, desc.params, 0)
+    rt.render(b.scene, 3, desc.params, 3)
+    split = rt.download()
+    cpu = load_cpu(desc, "port").render_pcg(desc)
+    assert relmse(split, cpu) <= TOL
+
+
+def test_fp64_film_and_clear(ctx):
+    from xitils_gb300 import api
+    desc = scenes.cornell(32, 32, 4)
+    b = api.load_scene(ctx, desc)
+    f32 = api.RenderTarget(ctx, 32, 32)
+    f64 = api.RenderTarget(ctx, 32, 32, fp64=True)
+    f32.render(b.scene, 4, desc.params)
+    f64.render(b.scene, 4, desc.params)
+    a, c = f32.download(), f64.download()
+    np.testing.assert_allclose(a, c, rtol=1e-4, atol=1e-5)
+    f64.clear()
+    assert f64.download().sum() == 0.0
+
+
+def test_small_queue_capacity_same_image(ctx):
+    """A queue far smaller than the work forces many refills; the film must not change beyond summation order."""
+    from xitils_gb300 import api
+    desc = scenes.cornell(40, 40, 4)
+    b = api.load_scene(ctx, desc)
+    big = api.RenderTarget(ctx, 40, 40)
+    big.render(b.scene, 4, desc.params)
+    p = IntegratorParams(max_depth=8, rr_start=3)
+    p.queue_capacity = 1024
+    small = api.RenderTarget(ctx, 40, 40)
+    small.render(b.scene, 4, p)
+    np.testing.assert_allclose(small.download(), big.download(), rtol=1e-4, atol=1e-5)
+    st = b.scene.stats()
+    assert st["paths"] == 40 * 40 * 4 and st["error_flags"] == 0

@@ -1,0 +1,425 @@
+"""Python binding of the C ABI (include/xgb.h) over ctypes.
+
+The classes mirror the reference's construction API so that a Xitils program
+reads the same: ``TriangleMesh.setGeometry``, ``Object(mesh, material,
+transform)``, ``Scene.addObject / buildAccelerationStructure``,
+``PinholeCamera``, the material classes, ``RenderTarget.render``. Everything
+runs on the GPU through libxgb.so; there is no CPU fallback -- constructing a
+``Context`` without the built library or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from .scene import (DIFFUSE, EMISSION, GLOSSY, GLOSSY_CLAMPED, GLOSSY_HIGHLIGHT, METAL, MF_NORMALMAP, NAIVE,
+                    SKY_LATLONG, SKY_NONE, SKY_PROBE, SKY_UNIFORM, SPECULAR_FRESNEL, SPECULAR_REFLECTION,
+                    SPECULAR_REFRACTION, STANDARD, IntegratorParams)
+from .transform import Transform
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libxgb.so")
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "QUEUE_OVERFLOW", 5: "DEVICE_TIMEOUT",
+          6: "NOT_BUILT", 7: "UNSUPPORTED"}
+
+
+class XgbError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class IntegratorParamsC(C.Structure):
+    _fields_ = [("integrator", C.c_int), ("max_depth", C.c_int), ("rr_start", C.c_int), ("rr_prob", C.c_float),
+                ("seed", C.c_uint32), ("queue_capacity", C.c_int)]
+
+
+class RenderStatsC(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("iterations", C.c_uint64), ("kernel_launches", C.c_uint64), ("node_visits", C.c_uint64),
+                ("tri_tests", C.c_uint64), ("error_flags", C.c_uint32), ("profiled", C.c_uint32),
+                ("kernel_ms", C.c_double * 5), ("stage_launches", C.c_uint64 * 5)]
+
+
+_lib = None
+P = C.c_void_p
+FP = C.POINTER(C.c_float)
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libxgb.so; raises if it has not been built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run __graft_entry__.build() (python -m xitils_gb300.build)")
+    lib = C.CDLL(path)
+    sig = {
+        "xgb_ctx_create": [C.c_int, C.POINTER(P)],
+        "xgb_ctx_destroy": [P],
+        "xgb_texture_create": [P, C.c_int, C.c_int, C.c_int, FP, C.c_int, C.c_int, C.POINTER(P)],
+        "xgb_texture_destroy": [P],
+        "xgb_mesh_create": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(P)],
+        "xgb_mesh_destroy": [P],
+        "xgb_mesh_triangle_count": [P, C.POINTER(C.c_int)],
+        "xgb_material_diffuse": [P, FP, P, C.POINTER(P)],
+        "xgb_material_metal": [P, C.c_float, FP, P, C.POINTER(P)],
+        "xgb_material_glossy": [P, FP, C.c_float, C.POINTER(P)],
+        "xgb_material_glossy_highlight": [P, FP, FP, C.c_float, C.c_float, C.c_float, C.POINTER(P)],
+        "xgb_material_glossy_clamped": [P, FP, C.c_float, C.POINTER(P)],
+        "xgb_material_emission": [P, FP, C.POINTER(P)],
+        "xgb_material_specular_reflection": [P, C.POINTER(P)],
+        "xgb_material_specular_refraction": [P, C.c_float, C.POINTER(P)],
+        "xgb_material_specular_fresnel": [P, C.c_float, C.POINTER(P)],
+        "xgb_material_mf_normalmap": [P, P, C.POINTER(P)],
+        "xgb_material_set_normalmap": [P, P],
+        "xgb_material_destroy": [P],
+        "xgb_scene_create": [P, C.POINTER(P)],
+        "xgb_scene_destroy": [P],
+        "xgb_scene_add_object": [P, P, P, FP, FP],
+        "xgb_scene_set_camera_pinhole": [P, FP, FP, C.c_float, C.c_float],
+        "xgb_scene_set_sky_none": [P],
+        "xgb_scene_set_sky_uniform": [P, FP],
+        "xgb_scene_set_sky_probe": [P, P],
+        "xgb_scene_set_sky_latlong": [P, P],
+        "xgb_scene_build": [P, P],
+        "xgb_film_create": [P, C.c_int, C.c_int, C.c_int, C.POINTER(P)],
+        "xgb_film_destroy": [P],
+        "xgb_film_clear": [P, P],
+        "xgb_film_download": [P, FP, C.c_int, P],
+        "xgb_film_device_pointer": [P, C.POINTER(P), C.POINTER(C.c_int)],
+        "xgb_render": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
+        "xgb_render_stats_get": [P, C.POINTER(RenderStatsC), P],
+        "xgb_scene_set_profiling": [P, C.c_int],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    lib.xgb_get_last_error.argtypes = [P]
+    lib.xgb_get_last_error.restype = C.c_char_p
+    lib.xgb_version.restype = C.c_char_p
+    lib.xgb_integrator_params_default.argtypes = [C.POINTER(IntegratorParamsC)]
+    lib.xgb_integrator_params_default.restype = None
+    _lib = lib
+    return lib
+
+
+def _f32(a, n=None) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if n is not None:
+        assert a.size == n
+    return a
+
+
+def _fp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(FP)
+
+
+class Context:
+    """One GPU (xgb_ctx_create)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = P()
+        st = self.lib.xgb_ctx_create(device, C.byref(h))
+        if st != 0:
+            raise XgbError(st, f"xgb_ctx_create({device}) failed (no CUDA device?)")
+        self.h = h
+        self._keep = []
+
+    def check(self, st: int, what: str = ""):
+        if st != 0:
+            msg = self.lib.xgb_get_last_error(self.h).decode()
+            raise XgbError(st, f"{what}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.xgb_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Texture:
+    """xitils::Texture built from float RGB texels [h, w, 3] (Texture.h:25-32)."""
+
+    def __init__(self, ctx: Context, rgb: np.ndarray, warpClamp: bool = True, filter: bool = True):
+        rgb = _f32(rgb)
+        h, w, ch = rgb.shape
+        self.ctx = ctx
+        self.h = P()
+        ctx.check(ctx.lib.xgb_texture_create(ctx.h, w, h, ch, _fp(rgb), int(warpClamp), int(filter), C.byref(self.h)),
+                  "Texture")
+
+
+class TriangleMesh:
+    """xitils::TriangleMesh; setGeometry copies the arrays and builds its BVH on the GPU."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = None
+        self.n_tris = 0
+
+    def setGeometry(self, positions, texCoords=None, normals=None, tangents=None, bitangents=None, indices=None):
+        pos = _f32(positions).reshape(-1, 3)
+        arr = lambda a, k: None if a is None else _f32(a).reshape(-1, k)
+        uv, n, t, b = arr(texCoords, 2), arr(normals, 3), arr(tangents, 3), arr(bitangents, 3)
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int32).reshape(-1))
+        self.h = P()
+        ctx = self.ctx
+        ctx.check(ctx.lib.xgb_mesh_create(ctx.h, pos.shape[0], _fp(pos), _fp(uv), _fp(n), _fp(t), _fp(b), 12, 8,
+                                          idx.size, idx.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(self.h)),
+                  "TriangleMesh.setGeometry")
+        self.n_tris = idx.size // 3
+        return self
+
+
+class Material:
+    def __init__(self, ctx: Context, maker, *args):
+        self.ctx = ctx
+        self.h = P()
+        ctx.check(maker(ctx.h, *args, C.byref(self.h)), type(self).__name__)
+        self.normalmap = None
+
+    def set_normalmap(self, tex: Optional[Texture]):
+        self.normalmap = tex
+        self.ctx.check(self.ctx.lib.xgb_material_set_normalmap(self.h, tex.h if tex else None), "normalmap")
+
+
+class Diffuse(Material):
+    def __init__(self, ctx, albedo, texture: Optional[Texture] = None):
+        a = _f32(albedo, 3)
+        super().__init__(ctx, ctx.lib.xgb_material_diffuse, _fp(a), texture.h if texture else None)
+
+
+class Metal(Material):
+    def __init__(self, ctx, roughness, f0, roughness_texture: Optional[Texture] = None):
+        f = _f32(f0, 3)
+        super().__init__(ctx, ctx.lib.xgb_material_metal, C.c_float(roughness), _fp(f),
+                         roughness_texture.h if roughness_texture else None)
+
+
+class Glossy(Material):
+    def __init__(self, ctx, albedo, sharpness):
+        super().__init__(ctx, ctx.lib.xgb_material_glossy, _fp(_f32(albedo, 3)), C.c_float(sharpness))
+
+
+class GlossyWithHighLight(Material):
+    def __init__(self, ctx, albedo, highlight, sharpness, sharpnessHighLight, highlightRate):
+        super().__init__(ctx, ctx.lib.xgb_material_glossy_highlight, _fp(_f32(albedo, 3)), _fp(_f32(highlight, 3)),
+                         C.c_float(sharpness), C.c_float(sharpnessHighLight), C.c_float(highlightRate))
+
+
+class GlossyClamped(Material):
+    def __init__(self, ctx, albedo, sharpness):
+        super().__init__(ctx, ctx.lib.xgb_material_glossy_clamped, _fp(_f32(albedo, 3)), C.c_float(sharpness))
+
+
+class Emission(Material):
+    def __init__(self, ctx, power):
+        super().__init__(ctx, ctx.lib.xgb_material_emission, _fp(_f32(power, 3)))
+
+
+class SpecularReflection(Material):
+    def __init__(self, ctx):
+        super().__init__(ctx, ctx.lib.xgb_material_specular_reflection)
+
+
+class SpecularRefraction(Material):
+    def __init__(self, ctx, index=1.0):
+        super().__init__(ctx, ctx.lib.xgb_material_specular_refraction, C.c_float(index))
+
+
+class SpecularFresnel(Material):
+    def __init__(self, ctx, index=1.0):
+        super().__init__(ctx, ctx.lib.xgb_material_specular_fresnel, C.c_float(index))
+
+
+class MicrofacetNormalMapping(Material):
+    def __init__(self, ctx, base: Material):
+        super().__init__(ctx, ctx.lib.xgb_material_mf_normalmap, base.h)
+        self.base = base
+
+
+class PinholeCamera:
+    def __init__(self, cameraToWorld: Transform, fov: float, aspectRatio: float):
+        self.cameraToWorld, self.fov, self.aspectRatio = cameraToWorld, float(fov), float(aspectRatio)
+
+
+class Object:
+    def __init__(self, shape: TriangleMesh, material: Material, objectToWorld: Optional[Transform] = None):
+        self.shape, self.material = shape, material
+        self.objectToWorld = objectToWorld or Transform.identity()
+
+
+class Scene:
+    """xitils::Scene: objects, camera and sky; buildAccelerationStructure uploads it."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = P()
+        ctx.check(ctx.lib.xgb_scene_create(ctx.h, C.byref(self.h)), "Scene")
+        self.objects = []
+        self.camera = None
+        self.skySphere = None
+        self._keep = []
+
+    def addObject(self, obj: Object):
+        m = _f32(obj.objectToWorld.mat, 16)
+        mi = _f32(obj.objectToWorld.matInv, 16)
+        self.ctx.check(self.ctx.lib.xgb_scene_add_object(self.h, obj.shape.h, obj.material.h, _fp(m), _fp(mi)),
+                       "addObject")
+        self.objects.append(obj)
+
+    def setCamera(self, cam: PinholeCamera):
+        m = _f32(cam.cameraToWorld.mat, 16)
+        mi = _f32(cam.cameraToWorld.matInv, 16)
+        self.ctx.check(self.ctx.lib.xgb_scene_set_camera_pinhole(self.h, _fp(m), _fp(mi), cam.fov, cam.aspectRatio),
+                       "camera")
+        self.camera = cam
+
+    def setSky(self, kind: int, rgb=None, tex: Optional[Texture] = None):
+        lib = self.ctx.lib
+        if kind == SKY_NONE:
+            st = lib.xgb_scene_set_sky_none(self.h)
+        elif kind == SKY_UNIFORM:
+            st = lib.xgb_scene_set_sky_uniform(self.h, _fp(_f32(rgb, 3)))
+        elif kind == SKY_PROBE:
+            st = lib.xgb_scene_set_sky_probe(self.h, tex.h)
+        elif kind == SKY_LATLONG:
+            st = lib.xgb_scene_set_sky_latlong(self.h, tex.h)
+        else:
+            raise ValueError(kind)
+        self.ctx.check(st, "sky")
+        self.skySphere = (kind, rgb, tex)
+
+    def buildAccelerationStructure(self, stream=None):
+        self.ctx.check(self.ctx.lib.xgb_scene_build(self.h, stream), "buildAccelerationStructure")
+
+    def set_profiling(self, enable: bool = True):
+        self.ctx.check(self.ctx.lib.xgb_scene_set_profiling(self.h, int(enable)), "set_profiling")
+
+    def stats(self, stream=None) -> dict:
+        s = RenderStatsC()
+        self.ctx.check(self.ctx.lib.xgb_render_stats_get(self.h, C.byref(s), stream), "stats")
+        out = {}
+        for k, _ in RenderStatsC._fields_:
+            v = getattr(s, k)
+            out[k] = list(v) if k in ("kernel_ms", "stage_launches") else int(v)
+        return out
+
+
+class RenderTarget:
+    """Per-pixel radiance sums on the GPU (RenderTarget<Vector3f>)."""
+
+    def __init__(self, ctx: Context, width: int, height: int, fp64: bool = False):
+        self.ctx, self.width, self.height = ctx, width, height
+        self.h = P()
+        ctx.check(ctx.lib.xgb_film_create(ctx.h, width, height, int(fp64), C.byref(self.h)), "RenderTarget")
+
+    def clear(self, stream=None):
+        self.ctx.check(self.ctx.lib.xgb_film_clear(self.h, stream), "clear")
+
+    def render(self, scene: Scene, sampleNum: int, params: Optional[IntegratorParams] = None, sampleBegin: int = 0,
+               stream=None):
+        p = params or IntegratorParams()
+        pc = IntegratorParamsC(p.integrator, p.max_depth, p.rr_start, p.rr_prob, p.seed, getattr(p, "queue_capacity", 0))
+        self.ctx.check(self.ctx.lib.xgb_render(scene.h, C.byref(pc), self.h, sampleBegin, sampleNum, stream), "render")
+
+    def download(self, out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == self.width * self.height * 3
+        self.ctx.check(self.ctx.lib.xgb_film_download(self.h, _fp(out), 12, stream), "download")
+        return out
+
+    def device_pointer(self):
+        p = P()
+        f = C.c_int()
+        self.ctx.check(self.ctx.lib.xgb_film_device_pointer(self.h, C.byref(p), C.byref(f)), "device_pointer")
+        return p.value, bool(f.value)
+
+
+class GpuSceneBuilder:
+    """Backend for ``SceneDesc.emit``: replays a recorded scene into the GPU library."""
+
+    KIND_MAKERS = {DIFFUSE, METAL, GLOSSY, GLOSSY_HIGHLIGHT, GLOSSY_CLAMPED, EMISSION, SPECULAR_REFLECTION,
+                   SPECULAR_REFRACTION, SPECULAR_FRESNEL, MF_NORMALMAP}
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.scene = Scene(ctx)
+        self.textures, self.meshes, self.materials = [], [], []
+
+    def add_texture(self, rgb, clamp=True, filter=True):
+        self.textures.append(Texture(self.ctx, rgb, clamp, filter))
+        return len(self.textures) - 1
+
+    def add_mesh(self, pos, idx, uv=None, nrm=None, tan=None, bit=None):
+        self.meshes.append(TriangleMesh(self.ctx).setGeometry(pos, uv, nrm, tan, bit, idx))
+        return len(self.meshes) - 1
+
+    def add_material(self, kind, f, base=-1, tex=-1, normalmap=-1):
+        ctx = self.ctx
+        t = self.textures[tex] if tex >= 0 else None
+        if kind == DIFFUSE:
+            m = Diffuse(ctx, f[:3], t)
+        elif kind == METAL:
+            m = Metal(ctx, f[0], f[1:4], t)
+        elif kind == GLOSSY:
+            m = Glossy(ctx, f[:3], f[3])
+        elif kind == GLOSSY_HIGHLIGHT:
+            m = GlossyWithHighLight(ctx, f[:3], f[3:6], f[6], f[7], f[8])
+        elif kind == GLOSSY_CLAMPED:
+            m = GlossyClamped(ctx, f[:3], f[3])
+        elif kind == EMISSION:
+            m = Emission(ctx, f[:3])
+        elif kind == SPECULAR_REFLECTION:
+            m = SpecularReflection(ctx)
+        elif kind == SPECULAR_REFRACTION:
+            m = SpecularRefraction(ctx, f[0])
+        elif kind == SPECULAR_FRESNEL:
+            m = SpecularFresnel(ctx, f[0])
+        elif kind == MF_NORMALMAP:
+            m = MicrofacetNormalMapping(ctx, self.materials[base])
+        else:
+            raise ValueError(kind)
+        if normalmap >= 0:
+            m.set_normalmap(self.textures[normalmap])
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def add_object(self, mesh, material, mat, matInv):
+        self.scene.addObject(Object(self.meshes[mesh], self.materials[material], Transform(np.asarray(mat, np.float32),
+                                                                                         np.asarray(matInv, np.float32))))
+
+    def set_camera(self, c2w, c2wInv, fov, aspect):
+        self.scene.setCamera(PinholeCamera(Transform(np.asarray(c2w, np.float32), np.asarray(c2wInv, np.float32)),
+                                           fov, aspect))
+
+    def set_sky(self, kind, rgb, tex):
+        self.scene.setSky(kind, rgb, self.textures[tex] if tex >= 0 else None)
+
+    def build(self):
+        self.scene.buildAccelerationStructure()
+
+
+def load_scene(ctx: Context, desc) -> GpuSceneBuilder:
+    return desc.emit(GpuSceneBuilder(ctx))
+
+
+def render_desc(ctx: Context, desc, spp_begin: int = 0, spp_count: Optional[int] = None, params=None,
+                builder: Optional[GpuSceneBuilder] = None) -> np.ndarray:
+    """Builds (or reuses) a scene and renders it; returns float32 [H, W, 3] sums."""
+    b = builder or load_scene(ctx, desc)
+    rt = RenderTarget(ctx, desc.width, desc.height)
+    rt.render(b.scene, desc.spp if spp_count is None else spp_count, params or desc.params, spp_begin)
+    return rt.download()

@@ -1,0 +1,995 @@
+// Host implementation of the C ABI declared in include/xgb.h.
+//
+// Scene flattening follows the reference's object model: Scene::addObject
+// (Scene.h:17-22) appends objects and collects emissive ones as lights in
+// insertion order; light-sampling constants are computed here once with the
+// reference's float arithmetic (TriangleMesh.h:193-235, Object.h:91-110,
+// Scene.h:40-55) instead of per sample. This file is compiled with
+// -ffp-contract=off so the host float arithmetic matches the reference's.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/xgb.h"
+#include "xgb_kernels.h"
+
+using namespace xgb;
+
+// ------------------------------------------------------------ host helpers --
+namespace {
+
+struct H3 {
+    float x = 0, y = 0, z = 0;
+};
+inline H3 h3(float a, float b, float c) { H3 r; r.x = a; r.y = b; r.z = c; return r; }
+inline H3 sub(H3 a, H3 b) { return h3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline float dotH(H3 a, H3 b) { return (a.x * b.x + a.y * b.y) + (a.z * b.z + 0.0f * 0.0f); }
+inline H3 scaleH(H3 a, float s) { return h3(a.x * s, a.y * s, a.z * s); }
+inline H3 normalizeH(H3 a) { float inv = 1.0f / std::sqrt(dotH(a, a)); return scaleH(a, inv); }
+inline H3 crossH(H3 a, H3 b) {  // Vector.h:637-654
+    double ax = a.x, ay = a.y, az = a.z, bx = b.x, by = b.y, bz = b.z;
+    return h3((float)(ay * bz - az * by), (float)(az * bx - ax * bz), (float)(ax * by - ay * bx));
+}
+inline H3 pointH(const float* m, H3 v) {  // Transform.h:61-72
+    float xp = m[0] * v.x + m[1] * v.y + m[2] * v.z + m[3];
+    float yp = m[4] * v.x + m[5] * v.y + m[6] * v.z + m[7];
+    float zp = m[8] * v.x + m[9] * v.y + m[10] * v.z + m[11];
+    float wp = m[12] * v.x + m[13] * v.y + m[14] * v.z + m[15];
+    if (wp == 1) return h3(xp, yp, zp);
+    float inv = 1.0f / wp;
+    return h3(xp * inv, yp * inv, zp * inv);
+}
+inline H3 normalH(const float* m, H3 v) {  // Transform.h:121-127
+    return normalizeH(h3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+                         m[8] * v.x + m[9] * v.y + m[10] * v.z));
+}
+inline float lengthH(H3 a) { return std::sqrt(dotH(a, a)); }
+
+struct Box {
+    float lo[3] = {INFINITY, INFINITY, INFINITY};
+    float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    void add(H3 p) {
+        lo[0] = std::min(lo[0], p.x); lo[1] = std::min(lo[1], p.y); lo[2] = std::min(lo[2], p.z);
+        hi[0] = std::max(hi[0], p.x); hi[1] = std::max(hi[1], p.y); hi[2] = std::max(hi[2], p.z);
+    }
+    void add(const Box& b) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], b.lo[k]); hi[k] = std::max(hi[k], b.hi[k]); }
+    }
+};
+
+bool isIdentity(const float* m) {
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c)
+            if (m[4 * r + c] != (r == c ? 1.0f : 0.0f)) return false;
+    return true;
+}
+
+template <class T>
+cudaError_t upload(T** dptr, const T* host, size_t count, cudaStream_t s) {
+    *dptr = nullptr;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void**)dptr, sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(*dptr, host, sizeof(T) * count, cudaMemcpyHostToDevice, s);
+}
+
+void dfree(const void* p) {
+    if (p) cudaFree((void*)p);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ handles --
+struct xgb_ctx {
+    int device = 0;
+    int numSMs = 1;
+    cudaStream_t stream = nullptr;
+    std::string err;
+};
+
+struct xgb_texture {
+    xgb_ctx* ctx;
+    int w = 0, h = 0, clamp = 1, filter = 1;
+    float4* d = nullptr;
+};
+
+struct xgb_mesh {
+    xgb_ctx* ctx;
+    int nV = 0, nTris = 0;
+    std::vector<H3> pos, nrm;  // host copies for light tables and bounds
+    std::vector<int> idx;
+    bool hasUV = false, hasN = false, hasT = false;
+    float4 *dPos = nullptr, *dNrm = nullptr, *dTan = nullptr, *dBit = nullptr, *dGnrm = nullptr;
+    float2* dUV = nullptr;
+    int* dIdx = nullptr;
+    float* dArea = nullptr;
+    Node2* dNodes = nullptr;
+    TriV* dTris = nullptr;
+    int rootIsLeaf = 1, rootLeaf = 0;
+    std::vector<float> triArea;  // TriangleIndexed::surfaceArea
+    float area = 0;              // TriangleMesh::calcSurfaceArea
+    Box bound;                   // TriangleMesh::bound over all vertices
+};
+
+struct xgb_material {
+    xgb_ctx* ctx;
+    Material m;
+    const xgb_texture* tex = nullptr;
+    const xgb_texture* normalmap = nullptr;
+    const xgb_material* base = nullptr;
+};
+
+struct xgb_film {
+    xgb_ctx* ctx;
+    int w = 0, h = 0, fp64 = 0;
+    void* d = nullptr;
+};
+
+struct SceneObject {
+    const xgb_mesh* mesh;
+    const xgb_material* material;
+    float mat[16], matInv[16];
+};
+
+struct RenderBuffers {
+    unsigned int capacity = 0;
+    PathQueue q[2];
+    HitQueue hits;
+    ShadowQueue shadow;
+    void* block = nullptr;
+};
+
+struct xgb_scene {
+    xgb_ctx* ctx;
+    std::vector<SceneObject> objects;
+    bool hasCamera = false;
+    float c2w[16], c2wInv[16];
+    float fov = 1, aspect = 1;
+    int skyKind = SKY_NONE;
+    float skyRGB[3] = {0, 0, 0};
+    const xgb_texture* skyTex = nullptr;
+    bool built = false;
+    // device copies
+    SceneDev sd;
+    std::vector<void*> allocations;
+    RenderBuffers rb;
+    Ctrl* ctrl = nullptr;
+    Ctrl* ctrlHost = nullptr;  // pinned
+    xgb_render_stats last{};
+    bool profiling = false;
+    std::vector<cudaEvent_t> events;  // profiling: 6 per wavefront iteration
+};
+
+static xgb_status fail(xgb_ctx* ctx, xgb_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+static xgb_status cudaFail(xgb_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, XGB_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define XGB_CUDA(ctx, call)                                         \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cudaFail((ctx), e_, #call);   \
+    } while (0)
+
+static cudaStream_t pick(xgb_ctx* ctx, void* s) { return s ? (cudaStream_t)s : ctx->stream; }
+
+extern "C" {
+
+const char* xgb_version(void) { return "xgb 0.1 sm_103a"; }
+
+const char* xgb_get_last_error(const xgb_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+xgb_status xgb_ctx_create(int device, xgb_ctx** out) {
+    if (!out) return XGB_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) return XGB_CUDA_ERROR;
+    if (cudaSetDevice(device) != cudaSuccess) return XGB_CUDA_ERROR;
+    auto* c = new xgb_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return XGB_CUDA_ERROR;
+    }
+    *out = c;
+    return XGB_OK;
+}
+
+xgb_status xgb_ctx_destroy(xgb_ctx* ctx) {
+    if (!ctx) return XGB_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return XGB_OK;
+}
+
+// ---------------------------------------------------------------- textures --
+xgb_status xgb_texture_create(xgb_ctx* ctx, int width, int height, int channels, const float* texels, int wrap_clamp,
+                              int filter, xgb_texture** out) {
+    if (!ctx || !out || !texels || width <= 0 || height <= 0 || (channels != 3 && channels != 4))
+        return fail(ctx, XGB_INVALID_ARG, "xgb_texture_create: bad arguments");
+    cudaSetDevice(ctx->device);
+    size_t n = (size_t)width * height;
+    std::vector<float4> t(n);
+    for (size_t i = 0; i < n; ++i)
+        t[i] = make_float4(texels[channels * i], texels[channels * i + 1], texels[channels * i + 2], 0.0f);
+    auto* tex = new xgb_texture();
+    tex->ctx = ctx;
+    tex->w = width; tex->h = height; tex->clamp = wrap_clamp ? 1 : 0; tex->filter = filter ? 1 : 0;
+    cudaError_t e = upload(&tex->d, t.data(), n, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        dfree(tex->d);
+        delete tex;
+        return cudaFail(ctx, e, "xgb_texture_create");
+    }
+    *out = tex;
+    return XGB_OK;
+}
+
+xgb_status xgb_texture_destroy(xgb_texture* tex) {
+    if (!tex) return XGB_INVALID_ARG;
+    dfree(tex->d);
+    delete tex;
+    return XGB_OK;
+}
+
+// ------------------------------------------------------------------ meshes --
+static void freeMesh(xgb_mesh* m) {
+    for (const void* p : {(const void*)m->dPos, (const void*)m->dNrm, (const void*)m->dTan, (const void*)m->dBit,
+                          (const void*)m->dGnrm, (const void*)m->dUV, (const void*)m->dIdx, (const void*)m->dArea,
+                          (const void*)m->dNodes, (const void*)m->dTris})
+        dfree(p);
+}
+
+xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                           const float* normals, const float* tangents, const float* bitangents, int vec3_stride,
+                           int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out) {
+    if (!ctx || !out) return XGB_INVALID_ARG;
+    if (vertex_count <= 0 || !positions || index_count <= 0 || index_count % 3 || !indices)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: need positions and a multiple of 3 indices");
+    if (vec3_stride != 12 && vec3_stride != 16) return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: vec3_stride must be 12 or 16");
+    if (uv_stride != 8 && uv_stride != 16) return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: uv_stride must be 8 or 16");
+    if ((tangents == nullptr) != (bitangents == nullptr))
+        return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: tangents and bitangents go together");
+    for (int i = 0; i < index_count; ++i)
+        if (indices[i] < 0 || indices[i] >= vertex_count)
+            return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: index out of range");
+    cudaSetDevice(ctx->device);
+    const int vs = vec3_stride / 4, us = uv_stride / 4;
+    auto* m = new xgb_mesh();
+    m->ctx = ctx;
+    m->nV = vertex_count;
+    m->nTris = index_count / 3;
+    m->idx.assign(indices, indices + index_count);
+    m->pos.resize(vertex_count);
+    std::vector<float4> p4(vertex_count), n4, t4, b4;
+    std::vector<float2> uv;
+    for (int i = 0; i < vertex_count; ++i) {
+        const float* p = positions + (size_t)vs * i;
+        m->pos[i] = h3(p[0], p[1], p[2]);
+        p4[i] = make_float4(p[0], p[1], p[2], 0.0f);
+        m->bound.add(m->pos[i]);
+    }
+    auto fill4 = [&](const float* a, std::vector<float4>& v) {
+        v.resize(vertex_count);
+        for (int i = 0; i < vertex_count; ++i) {
+            const float* q = a + (size_t)vs * i;
+            v[i] = make_float4(q[0], q[1], q[2], 0.0f);
+        }
+    };
+    if (normals) {
+        fill4(normals, n4);
+        m->hasN = true;
+        m->nrm.resize(vertex_count);
+        for (int i = 0; i < vertex_count; ++i) m->nrm[i] = h3(n4[i].x, n4[i].y, n4[i].z);
+    }
+    if (tangents) { fill4(tangents, t4); fill4(bitangents, b4); m->hasT = true; }
+    if (texcoords) {
+        uv.resize(vertex_count);
+        for (int i = 0; i < vertex_count; ++i) uv[i] = make_float2(texcoords[(size_t)us * i], texcoords[(size_t)us * i + 1]);
+        m->hasUV = true;
+    }
+    // TriangleIndexed::surfaceArea (TriangleIndexed.h:56-62), TriangleMesh::calcSurfaceArea (:253-258)
+    m->triArea.resize(m->nTris);
+    m->area = 0.0f;
+    for (int t = 0; t < m->nTris; ++t) {
+        H3 a = m->pos[m->idx[3 * t]], b = m->pos[m->idx[3 * t + 1]], c = m->pos[m->idx[3 * t + 2]];
+        m->triArea[t] = lengthH(crossH(sub(b, a), sub(c, a))) / 2.0f;
+        m->area += m->triArea[t];
+    }
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = upload(&m->dPos, p4.data(), p4.size(), s);
+    if (e == cudaSuccess && m->hasN) e = upload(&m->dNrm, n4.data(), n4.size(), s);
+    if (e == cudaSuccess && m->hasT) e = upload(&m->dTan, t4.data(), t4.size(), s);
+    if (e == cudaSuccess && m->hasT) e = upload(&m->dBit, b4.data(), b4.size(), s);
+    if (e == cudaSuccess && m->hasUV) e = upload(&m->dUV, uv.data(), uv.size(), s);
+    if (e == cudaSuccess) e = upload(&m->dIdx, m->idx.data(), m->idx.size(), s);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->dGnrm, sizeof(float4) * m->nTris);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->dArea, sizeof(float) * m->nTris);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->dTris, sizeof(TriV) * m->nTris);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&m->dNodes, sizeof(Node2) * std::max(1, m->nTris - 1));
+    if (e == cudaSuccess) {
+        BlasBuildInput in{m->dPos, m->dIdx, m->nTris};
+        BlasBuildOutput o{};
+        o.nodes = m->dNodes; o.tris = m->dTris; o.gnrm = m->dGnrm; o.triArea = m->dArea;
+        e = buildBlas(in, &o, s);
+        m->rootIsLeaf = o.rootIsLeaf;
+        m->rootLeaf = o.rootLeaf;
+    }
+    if (e != cudaSuccess) {
+        freeMesh(m);
+        delete m;
+        return e == cudaErrorMemoryAllocation ? fail(ctx, XGB_OOM, "xgb_mesh_create: out of device memory")
+                                              : cudaFail(ctx, e, "xgb_mesh_create");
+    }
+    *out = m;
+    return XGB_OK;
+}
+
+xgb_status xgb_mesh_destroy(xgb_mesh* mesh) {
+    if (!mesh) return XGB_INVALID_ARG;
+    freeMesh(mesh);
+    delete mesh;
+    return XGB_OK;
+}
+
+xgb_status xgb_mesh_triangle_count(const xgb_mesh* mesh, int* out) {
+    if (!mesh || !out) return XGB_INVALID_ARG;
+    *out = mesh->nTris;
+    return XGB_OK;
+}
+
+// --------------------------------------------------------------- materials --
+static xgb_status newMaterial(xgb_ctx* ctx, int kind, xgb_material** out, xgb_material** made) {
+    if (!ctx || !out) return fail(ctx, XGB_INVALID_ARG, "material: null argument");
+    auto* m = new xgb_material();
+    m->ctx = ctx;
+    std::memset(&m->m, 0, sizeof(Material));
+    m->m.kind = kind;
+    m->m.tex = -1; m->m.normalmap = -1; m->m.base = -1;
+    m->m.index = 1.0f;
+    *made = m;
+    *out = m;
+    return XGB_OK;
+}
+static bool finite3(const float* v) { return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+xgb_status xgb_material_diffuse(xgb_ctx* ctx, const float albedo[3], const xgb_texture* albedo_tex, xgb_material** out) {
+    if (!finite3(albedo)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_diffuse: bad albedo");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_DIFFUSE, out, &m);
+    if (st) return st;
+    m->m.albedo = make_float3(albedo[0], albedo[1], albedo[2]);
+    m->tex = albedo_tex;
+    return XGB_OK;
+}
+xgb_status xgb_material_metal(xgb_ctx* ctx, float roughness, const float f0[3], const xgb_texture* roughness_tex,
+                              xgb_material** out) {
+    if (!finite3(f0) || !std::isfinite(roughness)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_metal: bad parameters");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_METAL, out, &m);
+    if (st) return st;
+    m->m.roughness = roughness;
+    m->m.albedo = make_float3(f0[0], f0[1], f0[2]);
+    m->tex = roughness_tex;
+    return XGB_OK;
+}
+xgb_status xgb_material_glossy(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out) {
+    if (!finite3(albedo)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_glossy: bad albedo");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_GLOSSY, out, &m);
+    if (st) return st;
+    m->m.albedo = make_float3(albedo[0], albedo[1], albedo[2]);
+    m->m.sharpness = sharpness;
+    return XGB_OK;
+}
+xgb_status xgb_material_glossy_highlight(xgb_ctx* ctx, const float albedo[3], const float highlight[3], float sharpness,
+                                         float sharpness_highlight, float rate, xgb_material** out) {
+    if (!finite3(albedo) || !finite3(highlight)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_glossy_highlight: bad colour");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_GLOSSY_HIGHLIGHT, out, &m);
+    if (st) return st;
+    m->m.albedo = make_float3(albedo[0], albedo[1], albedo[2]);
+    m->m.highlight = make_float3(highlight[0], highlight[1], highlight[2]);
+    m->m.sharpness = sharpness;
+    m->m.sharpnessHL = sharpness_highlight;
+    m->m.rate = rate;
+    return XGB_OK;
+}
+xgb_status xgb_material_glossy_clamped(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out) {
+    if (!finite3(albedo)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_glossy_clamped: bad albedo");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_GLOSSY_CLAMPED, out, &m);
+    if (st) return st;
+    m->m.albedo = make_float3(albedo[0], albedo[1], albedo[2]);
+    m->m.sharpness = sharpness;
+    return XGB_OK;
+}
+xgb_status xgb_material_emission(xgb_ctx* ctx, const float power[3], xgb_material** out) {
+    if (!finite3(power)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_emission: bad power");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_EMISSION, out, &m);
+    if (st) return st;
+    m->m.albedo = make_float3(power[0], power[1], power[2]);
+    return XGB_OK;
+}
+xgb_status xgb_material_specular_reflection(xgb_ctx* ctx, xgb_material** out) {
+    xgb_material* m;
+    return newMaterial(ctx, MAT_SPECULAR_REFLECTION, out, &m);
+}
+xgb_status xgb_material_specular_refraction(xgb_ctx* ctx, float index, xgb_material** out) {
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_SPECULAR_REFRACTION, out, &m);
+    if (st) return st;
+    m->m.index = index;
+    return XGB_OK;
+}
+xgb_status xgb_material_specular_fresnel(xgb_ctx* ctx, float index, xgb_material** out) {
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_SPECULAR_FRESNEL, out, &m);
+    if (st) return st;
+    m->m.index = index;
+    return XGB_OK;
+}
+xgb_status xgb_material_mf_normalmap(xgb_ctx* ctx, const xgb_material* base, xgb_material** out) {
+    if (!base || base->m.kind == MAT_MF_NORMALMAP || base->m.kind == MAT_EMISSION)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_material_mf_normalmap: base must be a non-emissive, non-MFNM material");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_MF_NORMALMAP, out, &m);
+    if (st) return st;
+    m->base = base;
+    return XGB_OK;
+}
+xgb_status xgb_material_set_normalmap(xgb_material* mat, const xgb_texture* normalmap) {
+    if (!mat) return XGB_INVALID_ARG;
+    mat->normalmap = normalmap;
+    return XGB_OK;
+}
+xgb_status xgb_material_destroy(xgb_material* mat) {
+    if (!mat) return XGB_INVALID_ARG;
+    delete mat;
+    return XGB_OK;
+}
+
+// ------------------------------------------------------------------- scene --
+static void freeSceneDevice(xgb_scene* s) {
+    for (void* p : s->allocations) dfree(p);
+    s->allocations.clear();
+    s->built = false;
+}
+static void freeBuffers(xgb_scene* s) {
+    dfree(s->rb.block);
+    s->rb = RenderBuffers();
+}
+
+xgb_status xgb_scene_create(xgb_ctx* ctx, xgb_scene** out) {
+    if (!ctx || !out) return XGB_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    auto* s = new xgb_scene();
+    s->ctx = ctx;
+    std::memset(&s->sd, 0, sizeof(SceneDev));
+    if (cudaMalloc((void**)&s->ctrl, sizeof(Ctrl)) != cudaSuccess ||
+        cudaMallocHost((void**)&s->ctrlHost, sizeof(Ctrl)) != cudaSuccess) {
+        dfree(s->ctrl);
+        delete s;
+        return fail(ctx, XGB_OOM, "xgb_scene_create: allocation failed");
+    }
+    *out = s;
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_destroy(xgb_scene* s) {
+    if (!s) return XGB_INVALID_ARG;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    freeSceneDevice(s);
+    freeBuffers(s);
+    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    dfree(s->ctrl);
+    if (s->ctrlHost) cudaFreeHost(s->ctrlHost);
+    delete s;
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_add_object(xgb_scene* s, const xgb_mesh* mesh, const xgb_material* material, const float mat[16],
+                                const float mat_inv[16]) {
+    if (!s || !mesh || !material || !mat || !mat_inv) return fail(s ? s->ctx : nullptr, XGB_INVALID_ARG, "xgb_scene_add_object: null argument");
+    SceneObject o;
+    o.mesh = mesh;
+    o.material = material;
+    std::memcpy(o.mat, mat, 64);
+    std::memcpy(o.matInv, mat_inv, 64);
+    s->objects.push_back(o);
+    s->built = false;
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_set_camera_pinhole(xgb_scene* s, const float c2w[16], const float c2w_inv[16], float fov,
+                                        float aspect) {
+    if (!s || !c2w || !c2w_inv || !(fov > 0.0f) || !std::isfinite(aspect))
+        return fail(s ? s->ctx : nullptr, XGB_INVALID_ARG, "xgb_scene_set_camera_pinhole: bad arguments");
+    std::memcpy(s->c2w, c2w, 64);
+    std::memcpy(s->c2wInv, c2w_inv, 64);
+    s->fov = fov;
+    s->aspect = aspect;
+    s->hasCamera = true;
+    // Camera.h:50-51, evaluated once on the host with the reference's float expressions.
+    std::memcpy(s->sd.c2w, c2w, 64);
+    s->sd.tanHalfX = tanf(fov / 2);
+    s->sd.tanHalfY = tanf(fov / 2 * aspect);
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_set_sky_none(xgb_scene* s) {
+    if (!s) return XGB_INVALID_ARG;
+    s->skyKind = SKY_NONE;
+    s->skyTex = nullptr;
+    s->built = false;
+    return XGB_OK;
+}
+xgb_status xgb_scene_set_sky_uniform(xgb_scene* s, const float rgb[3]) {
+    if (!s || !finite3(rgb)) return XGB_INVALID_ARG;
+    s->skyKind = SKY_UNIFORM;
+    std::memcpy(s->skyRGB, rgb, 12);
+    s->skyTex = nullptr;
+    s->built = false;
+    return XGB_OK;
+}
+xgb_status xgb_scene_set_sky_probe(xgb_scene* s, const xgb_texture* probe) {
+    if (!s || !probe) return XGB_INVALID_ARG;
+    s->skyKind = SKY_PROBE;
+    s->skyTex = probe;
+    s->built = false;
+    return XGB_OK;
+}
+xgb_status xgb_scene_set_sky_latlong(xgb_scene* s, const xgb_texture* latlong) {
+    if (!s || !latlong) return XGB_INVALID_ARG;
+    s->skyKind = SKY_LATLONG;
+    s->skyTex = latlong;
+    s->built = false;
+    return XGB_OK;
+}
+
+// Transform::operator()(Bounds3f) (Transform.h:155-178), padded by a relative
+// 1e-6 so that rounding never makes an instance box cull its own triangles.
+static Box transformBox(const float* m, const Box& b) {
+    H3 lo = h3(b.lo[0], b.lo[1], b.lo[2]);
+    H3 size = h3(b.hi[0] - b.lo[0], b.hi[1] - b.lo[1], b.hi[2] - b.lo[2]);
+    H3 tmin = pointH(m, lo);
+    H3 bx = h3(m[0], m[4], m[8]), by = h3(m[1], m[5], m[9]), bz = h3(m[2], m[6], m[10]);
+    H3 vx = scaleH(bx, size.x), vy = scaleH(by, size.y), vz = scaleH(bz, size.z);
+    auto add = [](H3 a, H3 c) { return h3(a.x + c.x, a.y + c.y, a.z + c.z); };
+    Box r;
+    r.add(tmin);
+    r.add(add(tmin, vx));
+    r.add(add(tmin, vy));
+    r.add(add(add(tmin, vy), vx));
+    r.add(add(tmin, vz));
+    r.add(add(add(tmin, vz), vx));
+    r.add(add(add(tmin, vz), vy));
+    r.add(add(add(add(tmin, vz), vy), vx));
+    for (int k = 0; k < 3; ++k) {
+        float pad = 1e-6f * (std::fabs(r.lo[k]) + std::fabs(r.hi[k]) + (r.hi[k] - r.lo[k])) + 1e-30f;
+        r.lo[k] -= pad;
+        r.hi[k] += pad;
+    }
+    return r;
+}
+
+// Top-level BVH over instance boxes: median split on the longest centroid axis.
+static int buildTlas(std::vector<Node2>& nodes, std::vector<int>& items, const std::vector<Box>& boxes, int begin,
+                     int end, Box* outBox) {
+    Box bb;
+    for (int i = begin; i < end; ++i) bb.add(boxes[items[i]]);
+    *outBox = bb;
+    if (end - begin == 1) return leafEncode(items[begin], 1);
+    Box cb;
+    for (int i = begin; i < end; ++i) {
+        const Box& b = boxes[items[i]];
+        cb.add(h3(0.5f * (b.lo[0] + b.hi[0]), 0.5f * (b.lo[1] + b.hi[1]), 0.5f * (b.lo[2] + b.hi[2])));
+    }
+    int axis = 0;
+    float ext = -1;
+    for (int k = 0; k < 3; ++k)
+        if (cb.hi[k] - cb.lo[k] > ext) { ext = cb.hi[k] - cb.lo[k]; axis = k; }
+    int mid = (begin + end) / 2;
+    std::nth_element(items.begin() + begin, items.begin() + mid, items.begin() + end, [&](int a, int b) {
+        return boxes[a].lo[axis] + boxes[a].hi[axis] < boxes[b].lo[axis] + boxes[b].hi[axis];
+    });
+    int me = (int)nodes.size();
+    nodes.push_back(Node2());
+    Box l, r;
+    int cl = buildTlas(nodes, items, boxes, begin, mid, &l);
+    int cr = buildTlas(nodes, items, boxes, mid, end, &r);
+    Node2& nd = nodes[me];
+    nd.a = make_float4(l.lo[0], l.lo[1], l.lo[2], l.hi[0]);
+    nd.b = make_float4(l.hi[1], l.hi[2], r.lo[0], r.lo[1]);
+    nd.c = make_float4(r.lo[2], r.hi[0], r.hi[1], r.hi[2]);
+    nd.d = make_int4(cl, cr, 0, 0);
+    return me;
+}
+
+xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
+    if (!s) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = s->ctx;
+    if (s->objects.empty()) return fail(ctx, XGB_INVALID_ARG, "xgb_scene_build: scene has no objects");
+    if (!s->hasCamera) return fail(ctx, XGB_INVALID_ARG, "xgb_scene_build: no camera");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick(ctx, stream);
+    XGB_CUDA(ctx, cudaStreamSynchronize(st));
+    freeSceneDevice(s);
+
+    // tables of meshes, materials and textures referenced by the objects
+    std::map<const xgb_mesh*, int> meshIds;
+    std::vector<const xgb_mesh*> meshes;
+    std::map<const xgb_material*, int> matIds;
+    std::vector<const xgb_material*> mats;
+    std::map<const xgb_texture*, int> texIds;
+    std::vector<const xgb_texture*> texs;
+    auto texId = [&](const xgb_texture* t) -> int {
+        if (!t) return -1;
+        auto it = texIds.find(t);
+        if (it != texIds.end()) return it->second;
+        texIds[t] = (int)texs.size();
+        texs.push_back(t);
+        return (int)texs.size() - 1;
+    };
+    std::function<int(const xgb_material*)> matId = [&](const xgb_material* m) -> int {
+        auto it = matIds.find(m);
+        if (it != matIds.end()) return it->second;
+        int base = m->base ? matId(m->base) : -1;
+        matIds[m] = (int)mats.size();
+        mats.push_back(m);
+        (void)base;
+        return (int)mats.size() - 1;
+    };
+    std::vector<Instance> inst(s->objects.size());
+    std::vector<Box> boxes(s->objects.size());
+    for (size_t i = 0; i < s->objects.size(); ++i) {
+        const SceneObject& o = s->objects[i];
+        if (!meshIds.count(o.mesh)) { meshIds[o.mesh] = (int)meshes.size(); meshes.push_back(o.mesh); }
+        std::memcpy(inst[i].mat, o.mat, 64);
+        std::memcpy(inst[i].matInv, o.matInv, 64);
+        inst[i].mesh = meshIds[o.mesh];
+        inst[i].material = matId(o.material);
+        inst[i].lightIndex = -1;
+        inst[i].identity = isIdentity(o.mat) && isIdentity(o.matInv) ? 1 : 0;
+        boxes[i] = transformBox(o.mat, o.mesh->bound);
+    }
+    std::vector<Material> dm(mats.size());
+    for (size_t i = 0; i < mats.size(); ++i) {
+        dm[i] = mats[i]->m;
+        dm[i].tex = texId(mats[i]->tex);
+        dm[i].normalmap = texId(mats[i]->normalmap);
+        dm[i].base = mats[i]->base ? matIds[mats[i]->base] : -1;
+    }
+    int skyTex = texId(s->skyTex);
+    std::vector<TextureDev> td(texs.size());
+    for (size_t i = 0; i < texs.size(); ++i) td[i] = TextureDev{texs[i]->d, texs[i]->w, texs[i]->h, texs[i]->clamp, texs[i]->filter};
+    std::vector<MeshDev> md(meshes.size());
+    for (size_t i = 0; i < meshes.size(); ++i) {
+        const xgb_mesh* m = meshes[i];
+        md[i] = MeshDev{m->dNodes, m->dTris, m->dPos, m->dUV, m->dNrm, m->dTan, m->dBit, m->dIdx, m->dGnrm, m->dArea,
+                        m->nTris, m->nV, m->rootIsLeaf, m->rootLeaf};
+    }
+
+    // lights (Scene.h:17-22) and their sampling constants
+    std::vector<LightDev> lights;
+    std::vector<float4> lightNormal;
+    std::vector<float> lightPdf;
+    for (size_t i = 0; i < s->objects.size(); ++i)
+        if (s->objects[i].material->m.kind == MAT_EMISSION) {
+            inst[i].lightIndex = (int)lights.size();
+            lights.push_back(LightDev{(int)i, inst[i].mesh, s->objects[i].mesh->nTris, 0});
+        }
+    for (auto& L : lights) {
+        const SceneObject& o = s->objects[L.instance];
+        const xgb_mesh* m = o.mesh;
+        L.triOffset = (int)lightPdf.size();
+        // TriangleMesh::surfaceAreaScaling (TriangleMesh.h:193-200, TriangleIndexed.h:64-72)
+        float scaled = 0.0f;
+        for (int t = 0; t < m->nTris; ++t) {
+            H3 a = pointH(o.mat, m->pos[m->idx[3 * t]]), b = pointH(o.mat, m->pos[m->idx[3 * t + 1]]),
+               c = pointH(o.mat, m->pos[m->idx[3 * t + 2]]);
+            float sc = lengthH(crossH(sub(b, a), sub(c, a))) / 2.0f / m->triArea[t];
+            scaled += m->triArea[t] * sc;
+        }
+        float scaling = scaled / m->area;
+        for (int t = 0; t < m->nTris; ++t) {
+            // pdf: TriangleIndexed.h:189 / TriangleMesh.h:221 / Object.h:96 / Scene.h:45
+            float pdf = 1.0f / m->triArea[t];
+            pdf /= m->nTris;
+            pdf /= scaling;
+            pdf /= lights.size();
+            lightPdf.push_back(pdf);
+            H3 a = m->pos[m->idx[3 * t]], b = m->pos[m->idx[3 * t + 1]], c = m->pos[m->idx[3 * t + 2]];
+            H3 n = normalH(o.mat, normalizeH(crossH(sub(b, a), sub(c, a))));
+            lightNormal.push_back(make_float4(n.x, n.y, n.z, 0.0f));
+        }
+    }
+
+    // top-level hierarchy
+    std::vector<Node2> tlas;
+    int tlasRootIsLeaf = 0;
+    if (inst.size() == 1) {
+        tlasRootIsLeaf = 1;
+        tlas.push_back(Node2());
+    } else {
+        std::vector<int> items(inst.size());
+        for (size_t i = 0; i < items.size(); ++i) items[i] = (int)i;
+        Box root;
+        buildTlas(tlas, items, boxes, 0, (int)items.size(), &root);
+    }
+
+    auto up = [&](auto** dptr, const auto& vec) -> cudaError_t {
+        cudaError_t e = upload(dptr, vec.data(), vec.size(), st);
+        if (*dptr) s->allocations.push_back((void*)*dptr);
+        return e;
+    };
+    SceneDev& sd = s->sd;
+    MeshDev* dMeshes; Instance* dInst; Node2* dTlas; Material* dMat; TextureDev* dTex = nullptr; LightDev* dLights = nullptr;
+    float4* dLN = nullptr; float* dLP = nullptr;
+    XGB_CUDA(ctx, up(&dMeshes, md));
+    XGB_CUDA(ctx, up(&dInst, inst));
+    XGB_CUDA(ctx, up(&dTlas, tlas));
+    XGB_CUDA(ctx, up(&dMat, dm));
+    XGB_CUDA(ctx, up(&dTex, td));
+    XGB_CUDA(ctx, up(&dLights, lights));
+    XGB_CUDA(ctx, up(&dLN, lightNormal));
+    XGB_CUDA(ctx, up(&dLP, lightPdf));
+    sd.meshes = dMeshes;
+    sd.instances = dInst;
+    sd.tlas = dTlas;
+    sd.nInstances = (int)inst.size();
+    sd.tlasRootIsLeaf = tlasRootIsLeaf;
+    sd.materials = dMat;
+    sd.textures = dTex;
+    sd.lights = dLights;
+    sd.nLights = (int)lights.size();
+    sd.lightNormal = dLN;
+    sd.lightPdf = dLP;
+    sd.skyKind = s->skyKind;
+    sd.skyTex = skyTex;
+    sd.skyColor = make_float3(s->skyRGB[0], s->skyRGB[1], s->skyRGB[2]);
+    XGB_CUDA(ctx, cudaStreamSynchronize(st));
+    s->built = true;
+    return XGB_OK;
+}
+
+// -------------------------------------------------------------------- film --
+xgb_status xgb_film_create(xgb_ctx* ctx, int width, int height, int fp64, xgb_film** out) {
+    if (!ctx || !out || width <= 0 || height <= 0) return fail(ctx, XGB_INVALID_ARG, "xgb_film_create: bad size");
+    cudaSetDevice(ctx->device);
+    auto* f = new xgb_film();
+    f->ctx = ctx;
+    f->w = width; f->h = height; f->fp64 = fp64 ? 1 : 0;
+    size_t bytes = (size_t)width * height * (f->fp64 ? 32 : 16);
+    cudaError_t e = cudaMalloc(&f->d, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->d, 0, bytes, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        dfree(f->d);
+        delete f;
+        return e == cudaErrorMemoryAllocation ? fail(ctx, XGB_OOM, "xgb_film_create: out of memory") : cudaFail(ctx, e, "xgb_film_create");
+    }
+    *out = f;
+    return XGB_OK;
+}
+xgb_status xgb_film_destroy(xgb_film* f) {
+    if (!f) return XGB_INVALID_ARG;
+    dfree(f->d);
+    delete f;
+    return XGB_OK;
+}
+xgb_status xgb_film_clear(xgb_film* f, void* stream) {
+    if (!f) return XGB_INVALID_ARG;
+    XGB_CUDA(f->ctx, cudaMemsetAsync(f->d, 0, (size_t)f->w * f->h * (f->fp64 ? 32 : 16), pick(f->ctx, stream)));
+    return XGB_OK;
+}
+xgb_status xgb_film_download(xgb_film* f, float* host, int stride, void* stream) {
+    if (!f || !host || (stride != 12 && stride != 16)) return fail(f ? f->ctx : nullptr, XGB_INVALID_ARG, "xgb_film_download: bad arguments");
+    cudaStream_t st = pick(f->ctx, stream);
+    size_t n = (size_t)f->w * f->h;
+    const int fs = stride / 4;
+    if (f->fp64) {
+        std::vector<double> tmp(4 * n);
+        XGB_CUDA(f->ctx, cudaMemcpyAsync(tmp.data(), f->d, 32 * n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
+        for (size_t i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) host[fs * i + k] = (float)tmp[4 * i + k];
+    } else if (stride == 16) {
+        XGB_CUDA(f->ctx, cudaMemcpyAsync(host, f->d, 16 * n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
+    } else {
+        XGB_CUDA(f->ctx, cudaMemcpy2DAsync(host, 12, f->d, 16, 12, n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
+    }
+    return XGB_OK;
+}
+xgb_status xgb_film_device_pointer(xgb_film* f, void** out, int* is_fp64) {
+    if (!f || !out) return XGB_INVALID_ARG;
+    *out = f->d;
+    if (is_fp64) *is_fp64 = f->fp64;
+    return XGB_OK;
+}
+
+// --------------------------------------------------------------- rendering --
+void xgb_integrator_params_default(xgb_integrator_params* p) {
+    if (!p) return;
+    p->integrator = XGB_INTEGRATOR_STANDARD;
+    p->max_depth = 0;
+    p->rr_start = 5;
+    p->rr_prob = 0.9f;
+    p->seed = 0;
+    p->queue_capacity = 0;
+}
+
+static xgb_status ensureBuffers(xgb_scene* s, unsigned int cap) {
+    if (s->rb.capacity >= cap && s->rb.block) return XGB_OK;
+    freeBuffers(s);
+    size_t pathBytes = (size_t)cap * (16 * 3 + 8);
+    size_t hitBytes = (size_t)cap * (16 + 4);
+    size_t shadowBytes = (size_t)cap * (16 * 3 + 8);
+    size_t total = 2 * pathBytes + hitBytes + shadowBytes + 64 * 16;
+    void* block = nullptr;
+    cudaError_t e = cudaMalloc(&block, total);
+    if (e != cudaSuccess) return fail(s->ctx, XGB_OOM, "render: cannot allocate path queues");
+    char* p = (char*)block;
+    auto take = [&](size_t bytes) { char* r = p; p += (bytes + 255) & ~(size_t)255; return r; };
+    for (int k = 0; k < 2; ++k) {
+        s->rb.q[k].o = (float4*)take(16 * (size_t)cap);
+        s->rb.q[k].d = (float4*)take(16 * (size_t)cap);
+        s->rb.q[k].thr = (float4*)take(16 * (size_t)cap);
+        s->rb.q[k].rng = (uint2*)take(8 * (size_t)cap);
+    }
+    s->rb.hits.h = (float4*)take(16 * (size_t)cap);
+    s->rb.hits.inst = (int*)take(4 * (size_t)cap);
+    s->rb.shadow.o = (float4*)take(16 * (size_t)cap);
+    s->rb.shadow.d = (float4*)take(16 * (size_t)cap);
+    s->rb.shadow.c = (float4*)take(16 * (size_t)cap);
+    s->rb.shadow.rng = (uint2*)take(8 * (size_t)cap);
+    s->rb.block = block;
+    s->rb.capacity = cap;
+    return XGB_OK;
+}
+
+xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_film* film, uint32_t spp_begin,
+                      uint32_t spp_count, void* stream) {
+    if (!s || !film) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = s->ctx;
+    if (!s->built) return fail(ctx, XGB_NOT_BUILT, "xgb_render: call xgb_scene_build first");
+    if (film->ctx != ctx) return fail(ctx, XGB_INVALID_ARG, "xgb_render: film belongs to another context");
+    xgb_integrator_params P;
+    if (params) P = *params;
+    else xgb_integrator_params_default(&P);
+    if (P.integrator != XGB_INTEGRATOR_STANDARD && P.integrator != XGB_INTEGRATOR_NAIVE)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_render: unknown integrator");
+    if (P.rr_start < 1 || !(P.rr_prob > 0.0f && P.rr_prob <= 1.0f) || P.max_depth < 0 || P.queue_capacity < 0)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_render: need rr_start >= 1, 0 < rr_prob <= 1, max_depth >= 0");
+    if (P.max_depth == 0 && P.rr_prob >= 1.0f)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_render: rr_prob = 1 needs a max_depth (paths would never end)");
+    if (P.max_depth > 60000) return fail(ctx, XGB_INVALID_ARG, "xgb_render: max_depth must be <= 60000");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick(ctx, stream);
+    s->last = xgb_render_stats{};
+    unsigned long long total = (unsigned long long)film->w * film->h * spp_count;
+    if (total == 0) return XGB_OK;
+    unsigned int cap = P.queue_capacity > 0 ? (unsigned int)P.queue_capacity : (1u << 21);
+    if ((unsigned long long)cap > total) cap = (unsigned int)std::max<unsigned long long>(total, 1024ull);
+    cap = (cap + 255u) & ~255u;
+    xgb_status bs = ensureBuffers(s, cap);
+    if (bs) return bs;
+    cap = s->rb.capacity;
+
+    RenderParams rp;
+    rp.width = film->w; rp.height = film->h;
+    rp.sppBegin = spp_begin;
+    rp.seed = P.seed;
+    rp.integrator = P.integrator;
+    rp.maxDepth = P.max_depth;
+    rp.rrStart = P.rr_start;
+    rp.rrProb = P.rr_prob;
+    rp.capacity = cap;
+    rp.filmFp64 = film->fp64;
+    rp.film = film->d;
+
+    Ctrl init;
+    std::memset(&init, 0, sizeof(init));
+    init.totalPaths = total;
+    *s->ctrlHost = init;
+    XGB_CUDA(ctx, cudaMemcpyAsync(s->ctrl, s->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, st));
+    const int gTrace = ctx->numSMs * extendBlocksPerSM();
+    const int gShadow = ctx->numSMs * shadowBlocksPerSM();
+    const int gShade = ctx->numSMs * 8;
+    int parity = 0;
+    const int kIterPerCheck = 8;
+    const bool prof = s->profiling;
+    if (prof && s->events.size() < 6 * kIterPerCheck) {
+        while (s->events.size() < 6 * kIterPerCheck) {
+            cudaEvent_t ev;
+            XGB_CUDA(ctx, cudaEventCreate(&ev));
+            s->events.push_back(ev);
+        }
+    }
+    double stageMs[5] = {0, 0, 0, 0, 0};
+    uint64_t launches = 0;
+    for (int guard = 0;; ++guard) {
+        for (int k = 0; k < kIterPerCheck; ++k) {
+            PathQueue& X = s->rb.q[parity];
+            PathQueue& Y = s->rb.q[parity ^ 1];
+            cudaEvent_t* ev = prof ? &s->events[6 * k] : nullptr;
+            if (prof) cudaEventRecord(ev[0], st);
+            launchPlan(s->ctrl, cap, st);
+            if (prof) cudaEventRecord(ev[1], st);
+            launchGenerate(s->sd, rp, X, s->ctrl, gShade, st);
+            if (prof) cudaEventRecord(ev[2], st);
+            launchExtend(s->sd, X, s->rb.hits, s->ctrl, gTrace, prof, st);
+            if (prof) cudaEventRecord(ev[3], st);
+            launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, gShade, st);
+            if (prof) cudaEventRecord(ev[4], st);
+            launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, gShadow, st);
+            if (prof) cudaEventRecord(ev[5], st);
+            launches += 5;
+            parity ^= 1;
+        }
+        XGB_CUDA(ctx, cudaGetLastError());
+        XGB_CUDA(ctx, cudaMemcpyAsync(s->ctrlHost, s->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(ctx, cudaStreamSynchronize(st));
+        if (prof) {
+            for (int k = 0; k < kIterPerCheck; ++k)
+                for (int j = 0; j < 5; ++j) {
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, s->events[6 * k + j], s->events[6 * k + j + 1]);
+                    stageMs[j] += ms;
+                }
+        }
+        const Ctrl& c = *s->ctrlHost;
+        if (c.nextPath >= c.totalPaths && c.nOut == 0) break;
+        if (guard > (1 << 22)) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: wavefront did not drain");
+    }
+    const Ctrl& c = *s->ctrlHost;
+    s->last.paths = c.pathsDone;
+    s->last.extension_rays = c.extensionRays;
+    s->last.shadow_rays = c.shadowRays;
+    s->last.iterations = c.iterations;
+    s->last.error_flags = c.errors;
+    s->last.kernel_launches = launches;
+    s->last.node_visits = c.nodeVisits;
+    s->last.tri_tests = c.triTests;
+    s->last.profiled = prof ? 1 : 0;
+    for (int j = 0; j < 5; ++j) {
+        s->last.kernel_ms[j] = stageMs[j];
+        s->last.stage_launches[j] = launches / 5;
+    }
+    if (c.errors & ERR_STACK) return fail(ctx, XGB_QUEUE_OVERFLOW, "xgb_render: traversal stack overflow");
+    if (c.errors & ERR_LOOP) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: traversal iteration bound exceeded");
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_set_profiling(xgb_scene* s, int enable) {
+    if (!s) return XGB_INVALID_ARG;
+    s->profiling = enable != 0;
+    return XGB_OK;
+}
+
+xgb_status xgb_render_stats_get(xgb_scene* s, xgb_render_stats* out, void* stream) {
+    if (!s || !out) return XGB_INVALID_ARG;
+    XGB_CUDA(s->ctx, cudaStreamSynchronize(pick(s->ctx, stream)));
+    *out = s->last;
+    return XGB_OK;
+}
+
+}  // extern "C"

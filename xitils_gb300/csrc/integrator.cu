@@ -1,0 +1,357 @@
+// Wavefront integrator: plan -> generate -> (extend, trace.cu) -> shade ->
+// (shadow, trace.cu), repeated until every camera path has finished.
+//
+// One iteration advances every path in flight by one vertex of
+// StandardPathTracer::eval (PathTracer.h:117-251) or NaivePathTracer::eval
+// (PathTracer.h:50-104). Paths are carried between iterations in a compacted
+// queue (warp ballot + one atomicAdd per warp); freed slots are refilled with
+// new camera paths, so the queue stays full until the work runs out.
+//
+// Per-path random numbers come from a PCG32 stream keyed by (pixel, sample),
+// drawn in the reference's order: film jitter x, y; then per vertex the
+// Russian-roulette draw, the BSDF sample, the light sample (object, triangle,
+// barycentrics) and, only when the light is visible, a stochastic bsdfCos.
+// This translation unit is compiled with -fmad=false.
+#include "materials.cuh"
+#include "xgb_kernels.h"
+
+namespace xgb {
+
+constexpr int kShadeBlock = 256;
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ void filmAddS(const RenderParams& rp, int pix, V3 c) {
+    if (rp.filmFp64) {
+        double* f = (double*)rp.film + 4 * (size_t)pix;
+        atomicAdd(f, (double)c.x);
+        atomicAdd(f + 1, (double)c.y);
+        atomicAdd(f + 2, (double)c.z);
+    } else {
+        atomicAdd((float4*)rp.film + pix, make_float4(c.x, c.y, c.z, 0.0f));
+    }
+}
+
+__global__ void k_plan(Ctrl* c, unsigned int capacity) {
+    unsigned int nCont = c->nOut;
+    unsigned long long remain = c->totalPaths - c->nextPath;
+    unsigned long long room = capacity - nCont;
+    unsigned int nNew = (unsigned int)(remain < room ? remain : room);
+    c->firstNew = c->nextPath;
+    c->nextPath += nNew;
+    c->nCont = nCont;
+    c->nActive = nCont + nNew;
+    c->nOut = 0;
+    c->nShadow = 0;
+    c->extendHead = 0;
+    c->shadowHead = 0;
+    if (c->nActive) c->iterations += 1;
+}
+
+// Camera paths: RenderTargetTile::GenerateFilmPosition (RenderTarget.h:68-80)
+// then PinholeCamera::generateRay (Camera.h:45-55).
+__global__ void __launch_bounds__(kShadeBlock) k_generate(SceneDev sc, RenderParams rp, PathQueue q, const Ctrl* ctrl) {
+    const unsigned int nCont = ctrl->nCont, nActive = ctrl->nActive;
+    const unsigned long long firstNew = ctrl->firstNew;
+    const unsigned int px = (unsigned int)rp.width * (unsigned int)rp.height;
+    for (unsigned int s = nCont + blockIdx.x * blockDim.x + threadIdx.x; s < nActive; s += gridDim.x * blockDim.x) {
+        unsigned long long g = firstNew + (s - nCont);
+        unsigned int sample = rp.sppBegin + (unsigned int)(g / px);
+        unsigned int pix = (unsigned int)(g % px);
+        int x = (int)(pix % (unsigned int)rp.width), y = (int)(pix / (unsigned int)rp.width);
+        Pcg rng;
+        rng.seed(pix, sample, rp.seed);
+        float fx = (float)x / (float)rp.width;
+        float fy = (float)y / (float)rp.height;
+        fy = 1.0f - fy;
+        fx = fx + (rng.randf() - 0.5f) / (float)rp.width;
+        fy = fy + (rng.randf() - 0.5f) / (float)rp.height;
+        V3 d = normalize(V3(sc.tanHalfX * (fx - 0.5f) * 2.0f, sc.tanHalfY * (fy - 0.5f) * 2.0f, 1.0f));
+        V3 o = xformPoint(sc.c2w, V3(0.0f, 0.0f, 0.0f));
+        d = xformVector(sc.c2w, d);
+        // Standard: the first loop vertex has pathLength 2; Naive counts from 1.
+        int len = rp.integrator == 0 ? 2 : 1;
+        q.o[s] = make_float4(o.x, o.y, o.z, 0.0f);
+        q.d[s] = make_float4(d.x, d.y, d.z, __int_as_float(len | (FLAG_PRIMARY << 16)));
+        q.thr[s] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float((int)pix));
+        q.rng[s] = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
+    }
+}
+
+// SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).
+__device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instance& in, int prim, float b0, float b1,
+                                               V3 dWorld) {
+    const MeshDev& m = sc.meshes[in.mesh];
+    int i0 = m.idx[3 * prim], i1 = m.idx[3 * prim + 1], i2 = m.idx[3 * prim + 2];
+    V3 p0 = v3(m.pos[i0]), p1 = v3(m.pos[i1]), p2 = v3(m.pos[i2]);
+    V3 dObj = in.identity ? dWorld : xformVector(in.matInv, dWorld);
+    Surface s;
+    s.uv = m.uv ? lerp3(m.uv[i0], m.uv[i1], m.uv[i2], b0, b1) : make_float2(0.0f, 0.0f);
+    s.p = lerp3(p0, p1, p2, b0, b1);
+    s.wo = normalize(-dObj);
+    s.n = m.nrm ? normalize(lerp3(v3(m.nrm[i0]), v3(m.nrm[i1]), v3(m.nrm[i2]), b0, b1)) : v3(m.gnrm[prim]);
+    s.sn = s.n;
+    if (m.tan) {
+        s.stan = normalize(lerp3(v3(m.tan[i0]), v3(m.tan[i1]), v3(m.tan[i2]), b0, b1));
+        s.sbit = normalize(lerp3(v3(m.bit[i0]), v3(m.bit[i1]), v3(m.bit[i2]), b0, b1));
+    } else {
+        s.stan = V3();
+        s.sbit = V3();
+    }
+    s.sn = faceForward(s.sn, s.wo);
+    // object -> world (an identity matrix product is exact, its normalize is not skipped)
+    if (!in.identity) s.p = xformPoint(in.mat, s.p);
+    s.n = in.identity ? normalize(s.n) : xformNormal(in.mat, s.n);
+    s.wo = in.identity ? normalize(s.wo) : xformNormal(in.mat, s.wo);
+    const Material& mat = sc.materials[in.material];
+    if (mat.normalmap >= 0) {
+        V3 nm = texLookup(sc.textures[mat.normalmap], s.uv.x, s.uv.y) * 2.0f - V3(1.0f);
+        s.sn = normalize(nm.z * s.sn + nm.x * s.stan + nm.y * s.sbit);
+    }
+    s.sn = in.identity ? normalize(s.sn) : xformNormal(in.mat, s.sn);
+    return s;
+}
+
+struct LightSampleD {
+    V3 p, n, sn;
+    float pdf;
+    int material;
+};
+
+// Scene::sampleSurface chain (Scene.h:40-47, Object.h:91-105,
+// TriangleMesh.h:216-230, TriangleIndexed.h:179-209).
+__device__ __forceinline__ LightSampleD sampleLight(const SceneDev& sc, Pcg& rng) {
+    const LightDev L = sc.lights[rng.randi(sc.nLights)];
+    const MeshDev& m = sc.meshes[L.mesh];
+    const Instance& in = sc.instances[L.instance];
+    int tri = rng.randi(L.nTris);
+    float t0, t1, t2, sum;
+    int tries = 0;
+    do {  // the reference retries without bound; three zero draws in a row never happen in practice
+        t0 = rng.randf(); t1 = rng.randf(); t2 = rng.randf();
+        sum = t0 + t1 + t2;
+    } while (sum == 0.0f && ++tries < 64);
+    float inv = 1.0f / sum;
+    t0 = t0 * inv;
+    t1 = t1 * inv;
+    int i0 = m.idx[3 * tri], i1 = m.idx[3 * tri + 1], i2 = m.idx[3 * tri + 2];
+    LightSampleD ls;
+    ls.p = lerp3(v3(m.pos[i0]), v3(m.pos[i1]), v3(m.pos[i2]), t0, t1);
+    if (!in.identity) ls.p = xformPoint(in.mat, ls.p);
+    ls.n = v3(sc.lightNormal[L.triOffset + tri]);
+    if (m.nrm) {
+        V3 sn = normalize(lerp3(v3(m.nrm[i0]), v3(m.nrm[i1]), v3(m.nrm[i2]), t0, t1));
+        ls.sn = in.identity ? normalize(sn) : xformNormal(in.mat, sn);
+    } else {
+        ls.sn = ls.n;
+    }
+    ls.pdf = sc.lightPdf[L.triOffset + tri];
+    ls.material = in.material;
+    return ls;
+}
+
+__device__ __forceinline__ V3 emission(const Material& m, V3 wo, V3 n) {  // Material.h:408-410
+    return dot(wo, n) > 0.0f ? V3(m.albedo.x, m.albedo.y, m.albedo.z) : V3();
+}
+
+constexpr float kRayOffset = 0.00001f;    // PathTracer.h:254
+constexpr float kShadowMargin = 0.0001f;  // PathTracer.h:257
+
+struct ShadeOut {
+    // continuing path
+    float4 o, d, thr;
+    uint2 rng;
+    // shadow ray
+    float4 so, sd, sc;
+    uint2 srng;
+    bool stochastic;
+};
+
+__global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams rp, PathQueue in, HitQueue hq,
+                                                       PathQueue out, ShadowQueue sq, Ctrl* ctrl) {
+    const unsigned int n = ctrl->nActive;
+    const int lane = threadIdx.x & 31;
+    const unsigned int warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned int nWarps = (gridDim.x * blockDim.x) >> 5;
+    const bool naive = rp.integrator == 1;
+    for (unsigned int base = warpId * 32u; base < n; base += nWarps * 32u) {
+        const unsigned int i = base + lane;
+        bool cont = false, shadow = false, done = false;
+        ShadeOut r;
+        r.stochastic = false;
+        if (i < n) {
+            float4 o4 = in.o[i], d4 = in.d[i], t4 = in.thr[i];
+            uint2 rs = in.rng[i];
+            float4 h = hq.h[i];
+            const int instId = hq.inst[i];
+            const int prim = __float_as_int(h.w);
+            const int meta = __float_as_int(d4.w);
+            int len = meta & 0xFFFF;
+            const int flags = meta >> 16;
+            const int pix = __float_as_int(t4.w);
+            const float pdfPrev = o4.w;
+            V3 dir(d4.x, d4.y, d4.z);
+            V3 thr(t4.x, t4.y, t4.z);
+            Pcg rng;
+            rng.state = ((uint64_t)rs.y << 32) | rs.x;
+            rng.inc = ((uint64_t)(unsigned int)pix << 1) | 1u;
+            if (prim < 0) {
+                // Miss: the sky, with no MIS (PathTracer.h:133-136, 192-197).
+                if (sc.skyKind != SKY_NONE) {
+                    V3 L = thr * skyRadiance(sc, dir);
+                    if (naive) L = clampPositive(L);  // PathTracer.h:96
+                    filmAddS(rp, pix, L);
+                }
+                done = true;
+            } else {
+                const Instance& inst = sc.instances[instId];
+                const Material& mat = sc.materials[inst.material];
+                Surface s = makeSurface(sc, inst, prim, h.y, h.z, dir);
+                const bool emissive = mat.kind == MAT_EMISSION;
+                if (naive) {
+                    // NaivePathTracer::eval (PathTracer.h:75-100): emission, BSDF sample,
+                    // then the next loop top (depth limit, Russian roulette) before tracing.
+                    if (emissive) filmAddS(rp, pix, thr * emission(mat, -dir, s.n));
+                    V3 wi;
+                    float pdf = pdfPrev;
+                    thr = thr * evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                    bool alive = !isZero(thr);
+                    len += 1;
+                    if (alive && rp.maxDepth > 0 && len > rp.maxDepth) alive = false;
+                    if (alive && len > rp.rrStart) {
+                        if (rng.randf() >= rp.rrProb) alive = false;
+                        else thr = thr / rp.rrProb;
+                    }
+                    if (alive) {
+                        V3 no = s.p + kRayOffset * wi;
+                        r.o = make_float4(no.x, no.y, no.z, pdf);
+                        r.d = make_float4(wi.x, wi.y, wi.z, __int_as_float(len));
+                        r.thr = make_float4(thr.x, thr.y, thr.z, __int_as_float(pix));
+                        r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
+                        cont = true;
+                    } else {
+                        done = true;
+                    }
+                } else if (flags & FLAG_PRIMARY) {
+                    if (emissive) filmAddS(rp, pix, thr * emission(mat, -dir, s.n));  // PathTracer.h:143-145
+                } else if (emissive) {
+                    // BSDF-sampled hit on an emitter (PathTracer.h:171-190).
+                    float mis;
+                    if (pdfPrev >= 0.0f && sc.nLights > 0) {
+                        float pl = sc.lightPdf[sc.lights[inst.lightIndex].triOffset + prim];
+                        float cosLight = fabsf(dot(dir, s.sn));
+                        float distSq = h.x * h.x;
+                        pl *= distSq / cosLight;
+                        mis = (pdfPrev * pdfPrev) / ((pdfPrev * pdfPrev) + (pl * pl));
+                    } else {
+                        mis = 1.0f;
+                    }
+                    if (mis > 0.0f) filmAddS(rp, pix, thr * mis * emission(mat, -dir, s.n));
+                }
+                // An emitter's evalAndSample is zero: the path ends there (its NEE
+                // contribution is multiplied by Emission::bsdfCos() == 0).
+                if (naive) {
+                    // handled above
+                } else if (emissive) {
+                    done = true;
+                } else if (rp.maxDepth > 0 && len > rp.maxDepth) {
+                    done = true;
+                } else {
+                    bool alive = true;
+                    if (len > rp.rrStart) {  // PathTracer.h:149-155
+                        if (rng.randf() >= rp.rrProb) alive = false;
+                        else thr = thr / rp.rrProb;
+                    }
+                    if (!alive) {
+                        done = true;
+                    } else {
+                        V3 wi;
+                        float pdf = pdfPrev;  // left untouched by materials that do not set it
+                        V3 f = evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                        if (!naive && sc.nLights > 0) {  // PathTracer.h:202-233
+                            LightSampleD ls = sampleLight(sc, rng);
+                            V3 toL = ls.p - s.p;
+                            float dist = length(toL);
+                            V3 sd = toL / dist;
+                            V3 so = s.p + kRayOffset * sd;
+                            float stMax = dist - kShadowMargin;
+                            if (dot(sd, ls.n) < 0) {
+                                float distSq = dist * dist;
+                                float mis;
+                                if (pdf >= 0.0f) {
+                                    float pb = getPDF(sc, mat, s, sd);
+                                    float cosLight = fabsf(dot(-sd, ls.sn));
+                                    pb *= cosLight / distSq;
+                                    mis = (ls.pdf * ls.pdf) / ((pb * pb) + (ls.pdf * ls.pdf));
+                                } else {
+                                    mis = 0.0f;
+                                }
+                                if (mis > 0.0f) {
+                                    float G = fabsf(dot(-sd, ls.sn)) / distSq;
+                                    Pcg spec = rng;  // bsdfCos draws only if the light is visible
+                                    V3 bc = bsdfCos(sc, mat, s, spec, sd);
+                                    V3 c = thr * mis * bc * emission(sc.materials[ls.material], -sd, ls.n) * G / ls.pdf;
+                                    r.so = make_float4(so.x, so.y, so.z, stMax);
+                                    r.sd = make_float4(sd.x, sd.y, sd.z, __int_as_float(pix));
+                                    r.sc = make_float4(c.x, c.y, c.z, 0.0f);
+                                    r.stochastic = spec.state != rng.state;
+                                    r.srng = make_uint2((unsigned int)spec.state, (unsigned int)(spec.state >> 32));
+                                    shadow = true;
+                                }
+                            }
+                        }
+                        V3 thrNext = thr * f;
+                        if (!isZero(f) && !isZero(thrNext)) {
+                            V3 no = s.p + kRayOffset * wi;
+                            r.o = make_float4(no.x, no.y, no.z, pdf);
+                            r.d = make_float4(wi.x, wi.y, wi.z, __int_as_float(len + 1));
+                            r.thr = make_float4(thrNext.x, thrNext.y, thrNext.z, __int_as_float(pix));
+                            r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
+                            cont = true;
+                        } else {
+                            done = true;
+                        }
+                    }
+                }
+            }
+        }
+        // compacted writes: continuing paths, then shadow rays (which may point at them)
+        unsigned int mc = __ballot_sync(kFull, cont);
+        unsigned int oc = 0;
+        if (lane == 0 && mc) oc = atomicAdd(&ctrl->nOut, (unsigned int)__popc(mc));
+        oc = __shfl_sync(kFull, oc, 0);
+        unsigned int slot = oc + __popc(mc & ((1u << lane) - 1u));
+        if (cont) {
+            out.o[slot] = r.o;
+            out.d[slot] = r.d;
+            out.thr[slot] = r.thr;
+            out.rng[slot] = r.rng;
+        }
+        unsigned int ms = __ballot_sync(kFull, shadow);
+        unsigned int os = 0;
+        if (lane == 0 && ms) os = atomicAdd(&ctrl->nShadow, (unsigned int)__popc(ms));
+        os = __shfl_sync(kFull, os, 0);
+        if (shadow) {
+            unsigned int ss = os + __popc(ms & ((1u << lane) - 1u));
+            sq.o[ss] = r.so;
+            sq.d[ss] = r.sd;
+            r.sc.w = __int_as_float((r.stochastic && cont) ? (int)slot : -1);
+            sq.c[ss] = r.sc;
+            sq.rng[ss] = r.srng;
+        }
+        unsigned int md = __ballot_sync(kFull, done);
+        if (lane == 0 && md) atomicAdd(&ctrl->pathsDone, (unsigned long long)__popc(md));
+    }
+}
+
+void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s) { k_plan<<<1, 1, 0, s>>>(ctrl, capacity); }
+
+void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s) {
+    k_generate<<<grid, kShadeBlock, 0, s>>>(sc, rp, q, ctrl);
+}
+
+void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
+                 Ctrl* ctrl, int grid, cudaStream_t s) {
+    k_shade<<<grid, kShadeBlock, 0, s>>>(sc, rp, in, h, out, sq, ctrl);
+}
+
+}  // namespace xgb

@@ -1,0 +1,401 @@
+// Materials, textures and skies on the device (Include/Xitils/Material.h,
+// Texture.h, SkySphere.h; Sandbox/MicrofacetBasedNormalMapping/Main.cpp:34-340).
+//
+// Expression order follows the reference; this header is compiled with
+// -fmad=false so float arithmetic is unfused as in the reference. Where the
+// reference promotes an intermediate to double (M_PI literals, pow(float, int)),
+// the device evaluates in float: results differ by at most a few ulp.
+#pragma once
+#include "xgb_math.cuh"
+#include "xgb_types.h"
+
+namespace xgb {
+
+struct Surface {  // SurfaceIntersection (Interaction.h:16-32), world space
+    V3 p, wo, n, sn, stan, sbit;
+    float2 uv;
+};
+
+// ---------------------------------------------------------------- textures --
+__device__ __forceinline__ V3 texAt(const TextureDev& t, int x, int y) {  // Texture.h:77-81, :161-171
+    if (t.clamp) {
+        x = x < 0 ? 0 : (x > t.w - 1 ? t.w - 1 : x);
+        y = y < 0 ? 0 : (y > t.h - 1 ? t.h - 1 : y);
+    } else {
+        x %= t.w; y %= t.h;
+        if (x < 0) x += t.w;
+        if (y < 0) y += t.h;
+    }
+    float4 v = __ldg(&t.texels[(size_t)x + (size_t)y * t.w]);
+    return V3(v.x, v.y, v.z);
+}
+__device__ __forceinline__ V3 texLookup(const TextureDev& t, float u, float v) {  // Texture.h:83-103
+    if (t.filter) {
+        float fx = u * (float)t.w - 0.5f, fy = v * (float)t.h - 0.5f;
+        int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+        int x1 = x0 + 1, y1 = y0 + 1;
+        float wx1 = fx - (float)x0, wy1 = fy - (float)y0;
+        float wx0 = 1.0f - wx1, wy0 = 1.0f - wy1;
+        return (wx0 * wy0) * texAt(t, x0, y0) + (wx0 * wy1) * texAt(t, x0, y1) + (wx1 * wy0) * texAt(t, x1, y0) +
+               (wx1 * wy1) * texAt(t, x1, y1);
+    }
+    return texAt(t, (int)(u * (float)t.w), (int)(v * (float)t.h));
+}
+
+// ------------------------------------------------------------------- skies --
+__device__ __forceinline__ V3 skyRadiance(const SceneDev& sc, V3 wi) {
+    switch (sc.skyKind) {
+    case SKY_UNIFORM: return V3(sc.skyColor.x, sc.skyColor.y, sc.skyColor.z);  // SkySphere.h:36-45
+    case SKY_PROBE: {  // SkySphereFromImage (SkySphere.h:14-34)
+        V3 d = normalize(-wi);
+        float sq = sqrtf(d.x * d.x + d.y * d.y);
+        if (sq == 0.0f) return V3();
+        float r = (1.0f / kPi) * acosf(d.z) / sq;
+        float u = (d.x * r + 1.0f) / 2.0f;
+        float v = (d.y * r + 1.0f) / 2.0f;
+        return texLookup(sc.textures[sc.skyTex], u, v);
+    }
+    case SKY_LATLONG: {
+        float u = atan2f(wi.x, -wi.z) * (0.5f / kPi) + 0.5f;
+        float cy = wi.y < -1.0f ? -1.0f : (wi.y > 1.0f ? 1.0f : wi.y);
+        float v = acosf(cy) * (1.0f / kPi);
+        return texLookup(sc.textures[sc.skyTex], u, v);
+    }
+    default: return V3();
+    }
+}
+
+// ------------------------------------------------------------------- Metal --
+struct MetalD {  // Material.h:275-384
+    float alpha;
+    V3 f0;
+    __device__ V3 F(V3 eye, V3 h) const { return f0 + (V3(1.0f) - f0) * powf(1 - dot(eye, h), 5.0f); }
+    __device__ float D(V3 x, V3 n) const {
+        float alpha2 = alpha * alpha;
+        float dn = dot(n, x);
+        float c2 = dn * dn;
+        float c4 = c2 * c2;
+        float tan2 = 1 / c2 - 1;
+        float s = alpha2 + tan2;
+        return alpha2 * (dn > 0 ? 1.0f : 0.0f) / (kPi * c4 * (s * s));
+    }
+    __device__ float G1(V3 x, V3 n) const {
+        float alpha2 = alpha * alpha;
+        float dn = dot(n, x);
+        float c2 = dn * dn;
+        float tan2 = 1 / c2 - 1;
+        float lambda = (-1 + safeSqrt(1 + alpha2 * tan2)) / 2;
+        return 1 / (1 + lambda);
+    }
+    __device__ float DV(V3 x, V3 n, V3 eye) const { return G1(eye, n) * clampPositive(dot(eye, x)) * D(x, n) / dot(eye, n); }
+    __device__ V3 sampleVNDF(V3 eye, V3 n, Pcg& rng) const {  // [Heitz 2018]
+        Basis basis(n);
+        V3 Ve = basis.fromGlobal(eye);
+        V3 Vh = normalize(V3(Ve.x, alpha * Ve.y, alpha * Ve.z));
+        float lensq = Vh.y * Vh.y + Vh.z * Vh.z;
+        V3 T1 = lensq > 0 ? V3(0, -Vh.z, Vh.y) / safeSqrt(lensq) : V3(0, 0, 1);
+        V3 T2 = cross(Vh, T1);
+        float U1 = rng.randf();
+        float U2 = rng.randf();
+        float r = sqrtf(U1);
+        float phi = 2.0f * kPi * U2;
+        float t1 = r * cosf(phi);
+        float t2 = r * sinf(phi);
+        float s = 0.5f * (1.0f + Vh.x);
+        t2 = (1.0f - s) * sqrtf(1.0f - t1 * t1) + s * t2;
+        V3 Nh = t1 * T1 + t2 * T2 + safeSqrt(1.0f - t1 * t1 - t2 * t2) * Vh;
+        V3 Ne = normalize(V3(clampPositive(Nh.x), alpha * Nh.y, alpha * Nh.z));
+        return basis.toGlobal(Ne);
+    }
+    __device__ V3 bsdfCos(const Surface& s, V3 wi) const {
+        V3 h = normalize(wi + s.wo);
+        V3 Fr = F(s.wo, h);
+        float Dv = D(h, s.sn);
+        float G = G1(wi, s.sn) * G1(s.wo, s.sn);
+        return Fr * Dv * G / clampPositive(4 * dot(s.wo, s.sn));
+    }
+    __device__ float pdf(const Surface& s, V3 wi) const {
+        V3 h = normalize(wi + s.wo);
+        return DV(h, s.sn, s.wo) / (4 * dot(s.wo, h));
+    }
+    __device__ V3 evalAndSample(const Surface& s, Pcg& rng, V3* wi, float* p) const {
+        V3 h = sampleVNDF(s.wo, s.sn, rng);
+        *wi = (2.0f * dot(s.wo, h)) * h - s.wo;
+        *p = pdf(s, *wi);
+        return bsdfCos(s, *wi) / *p;
+    }
+};
+
+// -------------------------------------------------------------- Glossy family --
+struct GlossyD {  // Material.h:88-132; clamped: Main.cpp:34-84
+    V3 albedo;
+    float sh;
+    bool clamped;
+    __device__ V3 bsdfCos(const Surface& s, V3 wi) const {
+        float N = 2 * kPi / (sh + 2);
+        if (clamped && !(dot(s.wo, s.sn) > 0.0f && dot(wi, s.sn) > 0.0f)) return V3(0.0f);
+        return albedo * powf(dot(normalize(s.wo + wi), s.sn), sh) / N;
+    }
+    __device__ float pdf(const Surface& s, V3 wi) const {
+        if (clamped && !(dot(s.wo, s.sn) > 0.0f && dot(wi, s.sn) > 0.0f)) return 0.0f;
+        return (sh + 1) / (2 * kPi) * powf(clampPositive(dot(normalize(s.wo + wi), s.sn)), sh);
+    }
+    __device__ V3 evalAndSample(const Surface& s, Pcg& rng, V3* wi, float* p) const {
+        float r1 = rng.randf();
+        float r2 = rng.randf();
+        Basis basis(s.sn);
+        float sq = safeSqrt(1 - powf(r2, 2 / (sh + 1.0f)));
+        float ph = 2 * kPi * r1;
+        V3 h = normalize(basis.toGlobal(powf(r2, 1 / (sh + 1.0f)), cosf(ph) * sq, sinf(ph) * sq));
+        *wi = -normalize(s.wo - (2.0f * dot(s.wo, h)) * h);
+        *p = pdf(s, *wi);
+        if (*p == 0.0f) return V3(0.0f);
+        return bsdfCos(s, *wi) / *p;
+    }
+};
+
+__device__ __forceinline__ float fresnelDielectric(V3 wo, V3 n, float eta_o, float eta_i) {  // Material.h:265-271
+    const float c = fabsf(dot(wo, n));
+    float r = eta_o / eta_i;
+    float g_sq = r * r - 1.0f + c * c;
+    if (g_sq <= 0.0f) return 1.0f;
+    float g = sqrtf(g_sq);
+    float a = (g - c) / (g + c);
+    float b = (c * (g + c) - 1.0f) / (c * (g - c) + 1.0f);
+    return 0.5f * (a * a) * (1.0f + b * b);
+}
+
+// ------------------------------------------------------- material dispatch --
+__device__ __forceinline__ float metalRoughness(const SceneDev& sc, const Material& m, const Surface& s) {
+    if (m.tex < 0) return m.roughness;
+    return texLookup(sc.textures[m.tex], s.uv.x, s.uv.y).x;
+}
+
+__device__ __forceinline__ V3 bsdfCosBasic(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    switch (m.kind) {
+    case MAT_DIFFUSE: {  // Material.h:59-65
+        V3 a = V3(m.albedo.x, m.albedo.y, m.albedo.z) / kPi;
+        if (m.tex >= 0) a = a * texLookup(sc.textures[m.tex], s.uv.x, s.uv.y);
+        return a * clampPositive(dot(s.sn, wi));
+    }
+    case MAT_METAL: {
+        float r = metalRoughness(sc, m, s);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.bsdfCos(s, wi);
+    }
+    case MAT_GLOSSY: return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false}.bsdfCos(s, wi);
+    case MAT_GLOSSY_CLAMPED: return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, true}.bsdfCos(s, wi);
+    case MAT_GLOSSY_HIGHLIGHT:
+        return (1.0f - m.rate) * GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false}.bsdfCos(s, wi) +
+               m.rate * GlossyD{V3(m.highlight.x, m.highlight.y, m.highlight.z), m.sharpnessHL, false}.bsdfCos(s, wi);
+    default: return V3();  // emission and delta BSDFs
+    }
+}
+
+__device__ __forceinline__ float pdfBasic(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    switch (m.kind) {
+    case MAT_DIFFUSE: return clampPositive(dot(wi, s.sn)) / kPi;  // Material.h:78-81
+    case MAT_METAL: {
+        float r = metalRoughness(sc, m, s);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.pdf(s, wi);
+    }
+    case MAT_GLOSSY: return GlossyD{V3(), m.sharpness, false}.pdf(s, wi);
+    case MAT_GLOSSY_CLAMPED: return GlossyD{V3(), m.sharpness, true}.pdf(s, wi);
+    case MAT_GLOSSY_HIGHLIGHT:
+        return (1.0f - m.rate) * GlossyD{V3(), m.sharpness, false}.pdf(s, wi) +
+               m.rate * GlossyD{V3(), m.sharpnessHL, false}.pdf(s, wi);
+    default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ V3 sampleBasic(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
+                                          float* pdf) {
+    switch (m.kind) {
+    case MAT_DIFFUSE: {  // Material.h:67-76, Vector.h:817-824
+        Basis basis(s.sn);
+        float u = rng.randf() * 1.0f;
+        float r = sqrtf(u);
+        float phi = rng.randf() * (2.0f * kPi);
+        *wi = basis.toGlobal(safeSqrt(1.0f - u), r * cosf(phi), r * sinf(phi));
+        *pdf = dot(*wi, s.sn) / kPi;
+        V3 a(m.albedo.x, m.albedo.y, m.albedo.z);
+        if (m.tex >= 0) a = a * texLookup(sc.textures[m.tex], s.uv.x, s.uv.y);
+        return a;
+    }
+    case MAT_METAL: {
+        float r = metalRoughness(sc, m, s);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.evalAndSample(s, rng, wi, pdf);
+    }
+    case MAT_GLOSSY:
+        return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false}.evalAndSample(s, rng, wi, pdf);
+    case MAT_GLOSSY_CLAMPED:
+        return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, true}.evalAndSample(s, rng, wi, pdf);
+    case MAT_GLOSSY_HIGHLIGHT: {  // Material.h:148-162
+        GlossyD base{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false};
+        GlossyD hl{V3(m.highlight.x, m.highlight.y, m.highlight.z), m.sharpnessHL, false};
+        V3 eval;
+        float tmp;
+        if (rng.randf() <= m.rate) {
+            V3 te = hl.evalAndSample(s, rng, wi, &tmp);
+            eval = (1.0f - m.rate) * base.bsdfCos(s, *wi) + m.rate * te;
+            *pdf = (1.0f - m.rate) * base.pdf(s, *wi) + m.rate * tmp;
+        } else {
+            V3 te = base.evalAndSample(s, rng, wi, &tmp);
+            eval = (1.0f - m.rate) * te + m.rate * hl.bsdfCos(s, *wi);
+            *pdf = (1.0f - m.rate) * tmp + m.rate * hl.pdf(s, *wi);
+        }
+        return eval;
+    }
+    case MAT_SPECULAR_REFLECTION:  // Material.h:180-187
+        *wi = -normalize(s.wo - (2.0f * dot(s.sn, s.wo)) * s.sn);
+        *pdf = -1.0f;
+        return V3(1.0f);
+    case MAT_SPECULAR_REFRACTION:
+    case MAT_SPECULAR_FRESNEL: {  // Material.h:196-250
+        float eta_i, eta_o;
+        if (dot(s.n, s.wo) > 0.0f) { eta_o = 1.0f; eta_i = m.index; }
+        else { eta_o = m.index; eta_i = 1.0f; }
+        bool reflect = false;
+        if (m.kind == MAT_SPECULAR_FRESNEL) reflect = fresnelDielectric(s.wo, s.sn, eta_o, eta_i) >= rng.randf();
+        if (reflect) {
+            *wi = -normalize(s.wo - (2.0f * dot(s.sn, s.wo)) * s.sn);
+        } else {
+            float rindex = eta_o / eta_i;
+            float c = dot(-s.wo, s.sn);
+            *wi = rindex * (-s.wo - c * s.sn) - safeSqrt(1 - (rindex * rindex) * (1 - c * c)) * s.sn;
+        }
+        *pdf = -1.0f;
+        return V3(1.0f);
+    }
+    default: return V3();  // Emission: zero, pdf untouched (Material.h:400-402)
+    }
+}
+
+// ---- MicrofacetNormalMapping, TangentFacetMode = SameMaterialExplicit ------
+struct MfnmFrame {
+    V3 wg, wp, wt;
+    int kind;  // 0: wg == wp (plain base), 1: wt is NaN, 2: full model
+};
+__device__ __forceinline__ MfnmFrame mfnmFrame(const Surface& s) {  // Main.cpp:97-115
+    MfnmFrame f;
+    f.wg = s.n;
+    f.wp = s.sn;
+    if (dot(s.wo, f.wg) < 0.0f) f.wg = f.wg * -1.0f;
+    if (dot(f.wg, f.wp) < 0.0f) f.wp = f.wp * -1.0f;
+    if (eq(f.wg, f.wp)) { f.kind = 0; return f; }
+    f.wt = normalize(cross(normalize(cross(f.wg, f.wp)), f.wg));
+    if (hasNan(f.wt)) { f.kind = 1; return f; }
+    if (dot(f.wp, f.wt) > 0) f.wt = f.wt * -1.0f;
+    f.kind = 2;
+    return f;
+}
+__device__ __forceinline__ float a_p(V3 w, V3 wp, V3 wg) { return clampPositive(dot(w, wp)) / fabsf(dot(wp, wg)); }
+__device__ __forceinline__ float a_t(V3 w, V3 wp, V3 wt, V3 wg) {
+    float d = dot(wp, wg);
+    return clampPositive(dot(w, wt)) * safeSqrt(1 - d * d) / fabsf(d);
+}
+__device__ __forceinline__ float lambda_p(V3 w, V3 wp, V3 wt, V3 wg) {
+    return a_p(w, wp, wg) / (a_p(w, wp, wg) + a_t(w, wp, wt, wg));
+}
+__device__ __forceinline__ float G1m(V3 w, V3 wm, V3 wp, V3 wt, V3 wg) {
+    return dot(w, wm) > 0.0f ? minf_ref(1.0f, clampPositive(dot(w, wg)) / (a_p(w, wp, wg) + a_t(w, wp, wt, wg))) : 0.0f;
+}
+
+__device__ __forceinline__ V3 bsdfCos(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
+    if (m.kind != MAT_MF_NORMALMAP) return bsdfCosBasic(sc, m, s, wi);
+    const Material& b = sc.materials[m.base];
+    MfnmFrame f = mfnmFrame(s);  // Main.cpp:94-171
+    if (f.kind == 0) return bsdfCosBasic(sc, b, s, wi);
+    if (f.kind == 1) return V3(0.0f);
+    V3 result(0.0f), weight(1.0f);
+    bool d = rng.randf() < lambda_p(s.wo, f.wp, f.wt, f.wg);
+    V3 wr = -s.wo;
+    Surface facet = s;
+    int i = 0;
+    float pdf;
+    while (true) {
+        V3 wm = d ? f.wp : f.wt;
+        facet.n = wm; facet.sn = wm; facet.wo = -wr;
+        result = result + weight * G1m(wi, wm, f.wp, f.wt, f.wg) * bsdfCosBasic(sc, b, facet, wi);
+        weight = weight * sampleBasic(sc, b, facet, rng, &wr, &pdf);
+        float g = G1m(wr, wm, f.wp, f.wt, f.wg);
+        if (rng.randf() < g) break;
+        d = !d;
+        if (isZero(weight)) break;
+        ++i;
+        if (i > 100) break;
+    }
+    return result;
+}
+
+__device__ __forceinline__ float getPDF(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    if (m.kind != MAT_MF_NORMALMAP) return pdfBasic(sc, m, s, wi);
+    const Material& b = sc.materials[m.base];
+    MfnmFrame f = mfnmFrame(s);  // Main.cpp:254-321
+    if (f.kind == 0) return pdfBasic(sc, b, s, wi);
+    if (f.kind == 1) return 1.0f;
+    float prob = lambda_p(s.wo, f.wp, f.wt, f.wg);
+    Surface facet = s;
+    float pdf = 0, diff = 0.0f;
+    float g_wi_wp = G1m(wi, f.wp, f.wp, f.wt, f.wg);
+    if (prob > 0.0f) {
+        facet.n = f.wp; facet.sn = f.wp;
+        pdf += prob * g_wi_wp * pdfBasic(sc, b, facet, wi);
+        diff += prob * (1.0f - g_wi_wp);
+    }
+    if (prob < 1.0f) {
+        facet.n = f.wt; facet.sn = f.wt;
+        float g_wi_wt = G1m(wi, f.wt, f.wp, f.wt, f.wg);
+        pdf += prob * g_wi_wt * pdfBasic(sc, b, facet, wi);
+        diff += prob * g_wi_wt;
+    }
+    return pdf + diff * clampPositive(dot(wi, f.wg)) / kPi;
+}
+
+// Returns material_eval = f * cos / pdf and samples wi (Material.h:22-28).
+// *pdf is left untouched where the reference leaves it untouched.
+__device__ __forceinline__ V3 evalAndSample(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
+                                            float* pdf) {
+    if (m.kind != MAT_MF_NORMALMAP) return sampleBasic(sc, m, s, rng, wi, pdf);
+    const Material& b = sc.materials[m.base];
+    MfnmFrame f = mfnmFrame(s);  // Main.cpp:173-252
+    if (f.kind == 0) return sampleBasic(sc, b, s, rng, wi, pdf);
+    if (f.kind == 1) return V3(0.0f);
+    V3 weight(1.0f);
+    bool d = rng.randf() < lambda_p(s.wo, f.wp, f.wt, f.wg);
+    V3 wr = -s.wo;
+    Surface facet = s;
+    int i = 0;
+    float tmppdf = 0.0f;
+    bool specular = true;
+    while (true) {
+        ++i;
+        V3 wm = d ? f.wp : f.wt;
+        facet.n = wm; facet.sn = wm; facet.wo = -wr;
+        weight = weight * sampleBasic(sc, b, facet, rng, &wr, &tmppdf);
+        if (tmppdf >= 0.0f) specular = false;
+        float g = G1m(wr, wm, f.wp, f.wt, f.wg);
+        if (rng.randf() < g) break;
+        d = !d;
+        if (isZero(weight)) break;
+        if (i > 100) { weight = weight * V3(0.0f); break; }
+    }
+    *wi = wr;
+    *pdf = !specular ? getPDF(sc, m, s, *wi) : -1.0f;
+    return V3(0.0f) + weight;
+}
+
+__device__ __forceinline__ V3 albedoOf(const SceneDev& sc, const Material& m, const Surface& s) {  // getAlbedo
+    switch (m.kind) {
+    case MAT_DIFFUSE: {
+        V3 a(m.albedo.x, m.albedo.y, m.albedo.z);
+        if (m.tex >= 0) a = a * texLookup(sc.textures[m.tex], s.uv.x, s.uv.y);
+        return a;
+    }
+    case MAT_METAL:
+    case MAT_GLOSSY:
+    case MAT_GLOSSY_HIGHLIGHT: return V3(m.albedo.x, m.albedo.y, m.albedo.z);
+    default: return V3();
+    }
+}
+
+}  // namespace xgb

@@ -1,0 +1,236 @@
+// Ray traversal: top-level BVH over instances, per-mesh BVH over triangles.
+//
+// Semantics follow the reference's Scene::intersect / intersectAny
+// (AccelerationStructure.h:94-156, Object.h:44-85, TriangleMesh.h:202-214):
+// the ray is moved into object space with the instance's inverse matrix
+// (Transform::inverse(Ray), Transform.h:151-153, direction not renormalised, so
+// t is shared), triangles are tested with the PBRT watertight test in FP32
+// (TriangleIndexed.h:75-177), and a hit is accepted while t <= tMax, tMax
+// shrinking to each accepted hit. The triangle test and the ray transform use
+// explicitly unfused IEEE operations (__fadd_rn / __fmul_rn), so their results
+// are bit-identical to the reference's float arithmetic; only the visiting
+// order differs (nearest child first), which changes nothing but ties.
+#pragma once
+#include "xgb_math.cuh"
+#include "xgb_types.h"
+
+namespace xgb {
+
+constexpr int kStackDepth = 64;
+// Upper bound on loop iterations of one traversal; a well-formed BVH never
+// comes close. Exceeding it sets error bit 4 and ends the traversal.
+constexpr int kMaxVisits = 1 << 22;
+
+struct TraceHit {
+    float t, b0, b1;
+    int prim;  // original triangle index, -1 on a miss
+    int inst;
+};
+
+struct WorkCount {
+    unsigned int nodes = 0;
+    unsigned int tris = 0;
+};
+
+__device__ __forceinline__ float pick(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+// Per-ray constants of the watertight test (TriangleIndexed.h:83-95).
+struct WRay {
+    float ox, oy, oz;
+    int kx, ky, kz;
+    float sx, sy, sz;
+    float ix, iy, iz;  // 1 / d for the slab test
+};
+
+__device__ __forceinline__ WRay makeWRay(V3 o, V3 d) {
+    WRay r;
+    r.ox = o.x; r.oy = o.y; r.oz = o.z;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax > ay && ax > az) ? 0 : ((ay > az) ? 1 : 2);
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    float dx = pick(d.x, d.y, d.z, kx), dy = pick(d.x, d.y, d.z, ky), dz = pick(d.x, d.y, d.z, kz);
+    r.sx = __fdiv_rn(-dx, dz);
+    r.sy = __fdiv_rn(-dy, dz);
+    r.sz = __fdiv_rn(1.0f, dz);
+    r.ix = 1.0f / d.x; r.iy = 1.0f / d.y; r.iz = 1.0f / d.z;
+    return r;
+}
+
+// TriangleIndexed::intersect, decision and barycentric part.
+__device__ __forceinline__ bool watertight(const WRay& r, float4 P0, float4 P1, float4 P2, float tMax, float& t,
+                                           float& b0, float& b1) {
+    float ax = __fsub_rn(P0.x, r.ox), ay = __fsub_rn(P0.y, r.oy), az = __fsub_rn(P0.z, r.oz);
+    float bx = __fsub_rn(P1.x, r.ox), by = __fsub_rn(P1.y, r.oy), bz = __fsub_rn(P1.z, r.oz);
+    float cx = __fsub_rn(P2.x, r.ox), cy = __fsub_rn(P2.y, r.oy), cz = __fsub_rn(P2.z, r.oz);
+    float p0x = pick(ax, ay, az, r.kx), p0y = pick(ax, ay, az, r.ky), p0z = pick(ax, ay, az, r.kz);
+    float p1x = pick(bx, by, bz, r.kx), p1y = pick(bx, by, bz, r.ky), p1z = pick(bx, by, bz, r.kz);
+    float p2x = pick(cx, cy, cz, r.kx), p2y = pick(cx, cy, cz, r.ky), p2z = pick(cx, cy, cz, r.kz);
+    p0x = __fadd_rn(p0x, __fmul_rn(r.sx, p0z)); p0y = __fadd_rn(p0y, __fmul_rn(r.sy, p0z));
+    p1x = __fadd_rn(p1x, __fmul_rn(r.sx, p1z)); p1y = __fadd_rn(p1y, __fmul_rn(r.sy, p1z));
+    p2x = __fadd_rn(p2x, __fmul_rn(r.sx, p2z)); p2y = __fadd_rn(p2y, __fmul_rn(r.sy, p2z));
+    float e0 = __fsub_rn(__fmul_rn(p1x, p2y), __fmul_rn(p1y, p2x));
+    float e1 = __fsub_rn(__fmul_rn(p2x, p0y), __fmul_rn(p2y, p0x));
+    float e2 = __fsub_rn(__fmul_rn(p0x, p1y), __fmul_rn(p0y, p1x));
+    if ((e0 < 0 || e1 < 0 || e2 < 0) && (e0 > 0 || e1 > 0 || e2 > 0)) return false;
+    float det = __fadd_rn(__fadd_rn(e0, e1), e2);
+    if (det == 0) return false;
+    p0z = __fmul_rn(p0z, r.sz); p1z = __fmul_rn(p1z, r.sz); p2z = __fmul_rn(p2z, r.sz);
+    float ts = __fadd_rn(__fadd_rn(__fmul_rn(e0, p0z), __fmul_rn(e1, p1z)), __fmul_rn(e2, p2z));
+    float lim = __fmul_rn(tMax, det);
+    if (det < 0 && (ts >= 0 || ts < lim)) return false;
+    if (det > 0 && (ts <= 0 || ts > lim)) return false;
+    float inv = __fdiv_rn(1.0f, det);
+    b0 = __fmul_rn(e0, inv);
+    b1 = __fmul_rn(e1, inv);
+    t = __fmul_rn(ts, inv);
+    return true;
+}
+
+// Slab test against [lo, hi] for t in [0, tMax]; NaN planes (0 * inf) are
+// ignored like the reference's comparisons ignore them (Bounds.h:176-191).
+// The far distance is widened by 2^-20 relative so that a box never culls a
+// triangle the watertight test would accept.
+__device__ __forceinline__ bool slab(const WRay& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                     float tMax, float& tNear) {
+    float tx0 = (lx - r.ox) * r.ix, tx1 = (hx - r.ox) * r.ix;
+    float ty0 = (ly - r.oy) * r.iy, ty1 = (hy - r.oy) * r.iy;
+    float tz0 = (lz - r.oz) * r.iz, tz1 = (hz - r.oz) * r.iz;
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tMax));
+    tNear = tn;
+    return tn <= tf * 1.00000095367431640625f;
+}
+
+__device__ __forceinline__ V3 xformPointRn(const float* m, V3 v) {
+    float xp = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[1], v.y)), __fmul_rn(m[2], v.z)), m[3]);
+    float yp = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[4], v.x), __fmul_rn(m[5], v.y)), __fmul_rn(m[6], v.z)), m[7]);
+    float zp = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[8], v.x), __fmul_rn(m[9], v.y)), __fmul_rn(m[10], v.z)), m[11]);
+    float wp = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[12], v.x), __fmul_rn(m[13], v.y)), __fmul_rn(m[14], v.z)), m[15]);
+    if (wp == 1.0f) return V3(xp, yp, zp);
+    float inv = __fdiv_rn(1.0f, wp);
+    return V3(__fmul_rn(xp, inv), __fmul_rn(yp, inv), __fmul_rn(zp, inv));
+}
+__device__ __forceinline__ V3 xformVectorRn(const float* m, V3 v) {
+    return V3(__fadd_rn(__fadd_rn(__fmul_rn(m[0], v.x), __fmul_rn(m[1], v.y)), __fmul_rn(m[2], v.z)),
+              __fadd_rn(__fadd_rn(__fmul_rn(m[4], v.x), __fmul_rn(m[5], v.y)), __fmul_rn(m[6], v.z)),
+              __fadd_rn(__fadd_rn(__fmul_rn(m[8], v.x), __fmul_rn(m[9], v.y)), __fmul_rn(m[10], v.z)));
+}
+
+// Traverses one mesh BVH. ANY: returns at the first accepted hit.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
+                                             unsigned int* errors, WorkCount& wc) {
+    int stack[kStackDepth];
+    int sp = 0;
+    int node = m.rootIsLeaf ? m.rootLeaf : 0;
+    bool found = false;
+    for (int guard = 0;; ++guard) {
+        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (node >= 0) {
+            if (COUNT) wc.nodes++;
+            const Node2* nd = m.nodes + node;
+            float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
+            int4 d = __ldg(&nd->d);
+            float t0, t1;
+            bool h0 = slab(r, a.x, a.y, a.z, a.w, b.x, b.y, tMax, t0);
+            bool h1 = slab(r, b.z, b.w, c.x, c.y, c.z, c.w, tMax, t1);
+            if (h0 && h1) {
+                int near = d.x, far = d.y;
+                if (t1 < t0) { near = d.y; far = d.x; }
+                if (sp >= kStackDepth) { atomicOr(errors, 1u); return found; }
+                stack[sp++] = far;
+                node = near;
+            } else if (h0) {
+                node = d.x;
+            } else if (h1) {
+                node = d.y;
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp];
+            }
+        } else {
+            int first = leafFirst(node), cnt = leafCount(node);
+            if (COUNT) wc.tris += cnt;
+            for (int k = 0; k < cnt; ++k) {
+                const TriV* tv = m.tris + first + k;
+                float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
+                float t, b0, b1;
+                if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+                    tMax = t;
+                    found = true;
+                    if (ANY) return true;
+                    hit.t = t; hit.b0 = b0; hit.b1 = b1;
+                    hit.prim = __float_as_int(p0.w);
+                    hit.inst = inst;
+                }
+            }
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    return found;
+}
+
+// Scene::intersect (ANY = false) / Scene::intersectAny (ANY = true).
+template <bool ANY, bool COUNT = false>
+__device__ __forceinline__ bool traceScene(const SceneDev& sc, V3 o, V3 d, float tMax, TraceHit& hit,
+                                           unsigned int* errors, WorkCount& wc) {
+    hit.prim = -1;
+    hit.inst = -1;
+    hit.t = tMax;
+    WRay wr = makeWRay(o, d);
+    int stack[16];
+    int sp = 0;
+    int node = sc.tlasRootIsLeaf ? leafEncode(0, 1) : 0;
+    bool found = false;
+    for (int guard = 0;; ++guard) {
+        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (node >= 0) {
+            if (COUNT) wc.nodes++;
+            const Node2* nd = sc.tlas + node;
+            float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
+            int4 dd = __ldg(&nd->d);
+            float t0, t1;
+            bool h0 = slab(wr, a.x, a.y, a.z, a.w, b.x, b.y, tMax, t0);
+            bool h1 = slab(wr, b.z, b.w, c.x, c.y, c.z, c.w, tMax, t1);
+            if (h0 && h1) {
+                int near = dd.x, far = dd.y;
+                if (t1 < t0) { near = dd.y; far = dd.x; }
+                if (sp >= 16) { atomicOr(errors, 1u); return found; }
+                stack[sp++] = far;
+                node = near;
+            } else if (h0) {
+                node = dd.x;
+            } else if (h1) {
+                node = dd.y;
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp];
+            }
+        } else {
+            int inst = leafFirst(node);
+            const Instance& in = sc.instances[inst];
+            const MeshDev& m = sc.meshes[in.mesh];
+            bool h;
+            if (in.identity) {
+                h = traverseBlas<ANY, COUNT>(m, wr, tMax, hit, inst, errors, wc);
+            } else {
+                V3 oo = xformPointRn(in.matInv, o);
+                V3 od = xformVectorRn(in.matInv, d);
+                WRay orr = makeWRay(oo, od);
+                h = traverseBlas<ANY, COUNT>(m, orr, tMax, hit, inst, errors, wc);
+            }
+            if (h) {
+                found = true;
+                if (ANY) return true;
+            }
+            if (sp == 0) break;
+            node = stack[--sp];
+        }
+    }
+    return found;
+}
+
+}  // namespace xgb

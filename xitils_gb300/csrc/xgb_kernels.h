@@ -1,0 +1,95 @@
+// Launch wrappers shared between the host API (api.cu) and the kernel
+// translation units. No CUDA types beyond cudaStream_t cross this boundary.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xgb_types.h"
+
+namespace xgb {
+
+// ---- BVH build (bvh_build.cu) ------------------------------------------------
+struct BlasBuildInput {
+    const float4* pos;  // device, object space
+    const int* idx;     // device, 3 per triangle
+    int nTris;
+};
+struct BlasBuildOutput {
+    Node2* nodes;       // device, nTris - 1 entries (nTris >= 2)
+    TriV* tris;         // device, nTris entries (leaf order)
+    float4* gnrm;       // device, nTris entries (original order)
+    float* triArea;     // device, nTris entries (original order)
+    int rootIsLeaf;
+    int rootLeaf;
+    float boundsLo[3], boundsHi[3];  // object-space bounds of the vertices used
+};
+// Builds a binary LBVH over the triangles on `stream` and synchronises it.
+// Returns a CUDA error code (cudaSuccess on success).
+cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream_t stream);
+
+// ---- wavefront (integrator.cu / trace.cu) --------------------------------------
+struct Ctrl {
+    unsigned long long nextPath;   // next camera path id to generate
+    unsigned long long totalPaths;
+    unsigned long long firstNew;   // id of the first path generated this iteration
+    unsigned int nCont;            // paths carried over into this iteration's input queue
+    unsigned int nActive;          // paths in this iteration's input queue
+    unsigned int nOut;             // paths written to the output queue by shade
+    unsigned int nShadow;          // shadow rays written by shade
+    unsigned int extendHead;       // persistent work counters
+    unsigned int shadowHead;
+    unsigned int errors;           // bit 0: traversal stack overflow
+    unsigned int pad;
+    unsigned long long extensionRays;
+    unsigned long long shadowRays;
+    unsigned long long iterations;
+    unsigned long long pathsDone;
+    unsigned long long nodeVisits;  // profiling counters (extension rays)
+    unsigned long long triTests;
+};
+
+enum ErrorBits : unsigned int { ERR_STACK = 1u, ERR_QUEUE = 2u, ERR_LOOP = 4u };
+
+struct PathQueue {
+    float4* o;    // o.xyz, w = pdf of the BSDF sample that produced this ray (-1: specular)
+    float4* d;    // d.xyz, w = bits: pathLength | flags << 16
+    float4* thr;  // throughput.xyz, w = bits: pixel index
+    uint2* rng;   // PCG state
+};
+struct HitQueue {
+    float4* h;    // t, b0, b1, bits(prim); prim = -1 on a miss
+    int* inst;
+};
+struct ShadowQueue {
+    float4* o;    // o.xyz, tMax
+    float4* d;    // d.xyz, bits(pixel)
+    float4* c;    // contribution rgb, bits(output-queue index of the path or -1)
+    uint2* rng;   // PCG state after a stochastic bsdfCos (committed if visible)
+};
+
+enum PathFlags : int { FLAG_PRIMARY = 1, FLAG_STOCHASTIC_NEE = 2 };
+
+struct RenderParams {
+    int width, height;
+    uint32_t sppBegin;
+    uint32_t seed;
+    int integrator;
+    int maxDepth;
+    int rrStart;
+    float rrProb;
+    unsigned int capacity;
+    int filmFp64;
+    void* film;  // float4* or double4*
+};
+
+void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s);
+void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
+void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int grid, bool count, cudaStream_t s);
+void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
+                 Ctrl* ctrl, int grid, cudaStream_t s);
+void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int grid,
+                  cudaStream_t s);
+int extendBlocksPerSM();
+int shadowBlocksPerSM();
+
+}  // namespace xgb

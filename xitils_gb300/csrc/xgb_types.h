@@ -1,0 +1,135 @@
+// Device data layout of a built scene (shared by host and device code).
+//
+// HBM layout, all arrays 16-byte aligned structure-of-arrays:
+//   per mesh (BLAS): Node2[] (64 B/node), TriV[] (48 B/triangle, leaf order),
+//     vertex attributes (float4 positions/normals/tangents/bitangents, float2 uv),
+//     int32 indices, float4 geometric normal per triangle (object space).
+//   per scene: Instance[] (mat, matInv, mesh, material), the top-level Node2[]
+//     over instances, Material[], Texture[] descriptors, Light[] tables.
+//   per render: path queues (2 x 64 B/path), hit records (32 B/path), shadow
+//     queue (48 B/path), a control block of counters.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace xgb {
+
+// Binary BVH node holding both children's boxes (one 64-byte line per visit).
+// child >= 0: inner node index; child < 0: leaf, ~child = (first << 4) | (count - 1).
+struct __align__(16) Node2 {
+    float4 a;  // c0.lo.x c0.lo.y c0.lo.z c0.hi.x
+    float4 b;  // c0.hi.y c0.hi.z c1.lo.x c1.lo.y
+    float4 c;  // c1.lo.z c1.hi.x c1.hi.y c1.hi.z
+    int4 d;    // child0 child1 - -
+};
+static_assert(sizeof(Node2) == 64, "Node2 size");
+
+constexpr int kLeafMax = 4;  // triangles per BLAS leaf
+
+__host__ __device__ inline int leafEncode(int first, int count) { return ~((first << 4) | (count - 1)); }
+__host__ __device__ inline int leafFirst(int code) { return (~code) >> 4; }
+__host__ __device__ inline int leafCount(int code) { return ((~code) & 15) + 1; }
+
+// Triangle vertices gathered in BVH leaf order: p0.xyz + original triangle index, p1, p2.
+struct __align__(16) TriV {
+    float4 p0;  // w = __int_as_float(original triangle index)
+    float4 p1;
+    float4 p2;
+};
+
+struct MeshDev {
+    const Node2* nodes;
+    const TriV* tris;
+    const float4* pos;   // object-space positions (w = 0)
+    const float2* uv;    // nullptr when absent
+    const float4* nrm;   // nullptr when absent
+    const float4* tan;   // nullptr when absent (then bit is nullptr too)
+    const float4* bit;
+    const int* idx;      // 3 per triangle
+    const float4* gnrm;  // normalize(cross(p1-p0, p2-p0)) per triangle, FP64 cross (Vector.h:637-654)
+    const float* triArea;  // TriangleIndexed::surfaceArea per triangle
+    int nTris;
+    int nVerts;
+    int rootIsLeaf;  // 1 when the whole mesh is a single leaf (nodes unused)
+    int rootLeaf;    // leaf code of that leaf
+};
+
+struct __align__(16) Instance {
+    float mat[16];     // object -> world, row-major m[r][c]
+    float matInv[16];  // world -> object
+    int mesh;
+    int material;
+    int lightIndex;    // index in the light table, -1 when not emissive
+    int identity;      // 1 when mat and matInv are exactly the identity
+};
+
+enum MaterialKind : int {
+    MAT_DIFFUSE = 0,
+    MAT_METAL = 1,
+    MAT_GLOSSY = 2,
+    MAT_GLOSSY_HIGHLIGHT = 3,
+    MAT_GLOSSY_CLAMPED = 4,
+    MAT_EMISSION = 5,
+    MAT_SPECULAR_REFLECTION = 6,
+    MAT_SPECULAR_REFRACTION = 7,
+    MAT_SPECULAR_FRESNEL = 8,
+    MAT_MF_NORMALMAP = 9,
+};
+
+struct __align__(16) Material {
+    int kind;
+    int tex;        // albedo texture (Diffuse) or roughness texture (Metal), -1 none
+    int normalmap;  // -1 none
+    int base;       // facet material (MicrofacetNormalMapping), -1 none
+    float3 albedo;  // albedo / f0 / power
+    float roughness;
+    float3 highlight;
+    float sharpness;
+    float sharpnessHL;
+    float rate;
+    float index;
+    float pad;
+};
+
+struct TextureDev {
+    const float4* texels;  // RGBA, row y = 0 first
+    int w, h;
+    int clamp;   // Texture::warpClamp
+    int filter;  // Texture::filter
+};
+
+enum SkyKind : int { SKY_NONE = 0, SKY_UNIFORM = 1, SKY_PROBE = 2, SKY_LATLONG = 3 };
+
+// One emissive object (Scene.h:17-22). Light triangle t of light L lives at
+// triOffset[L] + t in the scene-wide light-triangle arrays.
+struct LightDev {
+    int instance;
+    int mesh;
+    int nTris;
+    int triOffset;
+};
+
+struct SceneDev {
+    const MeshDev* meshes;
+    const Instance* instances;
+    const Node2* tlas;
+    int nInstances;
+    int tlasRootIsLeaf;
+    const Material* materials;
+    const TextureDev* textures;
+    const LightDev* lights;
+    int nLights;
+    // per light triangle (world data precomputed with the reference's arithmetic):
+    const float4* lightNormal;  // world geometric normal (Object.h:99 asNormal of the triangle normal)
+    const float* lightPdf;      // area pdf: 1/A / nTris / surfaceAreaScaling / nLights (Scene.h:40-55)
+    // camera (Camera.h:45-55)
+    float c2w[16];
+    float tanHalfX;  // tanf(fov/2)
+    float tanHalfY;  // tanf(fov/2 * aspect)
+    // sky (SkySphere.h)
+    int skyKind;
+    int skyTex;
+    float3 skyColor;
+};
+
+}  // namespace xgb

@@ -72,6 +72,7 @@ class IntegratorParams:
     rr_start: int = 5
     rr_prob: float = 0.9
     seed: int = 0
+    queue_capacity: int = 0
 
 
 @dataclass
