@@ -40,12 +40,16 @@ L2_BYTES = 129 * 1024 * 1024
 EXTEND_BYTES_PER_RAY = 52
 # BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
 NODE_BYTES, TRI_BYTES = 64, 48
+# DRAM bytes per extension ray of k_extend from one ncu capture on this scene
+# (profiles/extend_terrain_ncu_full.md: ~600 MB per ~2.03 M rays, 512x512x16 case,
+# same 2.09 M-triangle BVH); scaled to the average launch for roofline.traffic.
+EXTEND_DRAM_BYTES_PER_RAY = 295.0
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="xgb", choices=["xgb", "reference"])
     p.add_argument("--workload", default="terrain", choices=["terrain", "cornell"])
@@ -117,7 +121,7 @@ class ClockSampler:
                 sm.append(float(r[1]))
                 mx = float(r[2])
                 for k, nm in enumerate(names):
-                    if "Active" in r[5 + k]:
+                    if r[5 + k].strip() == "Active":
                         reasons.add(nm)
             except Exception:
                 continue
@@ -204,7 +208,7 @@ def run_xgb(args):
     sptr = C.c_void_p(stream.cuda_stream)
     params = desc.params
     step_paths = W * H * spp
-    sample_base = rank * spp * (args.warmup + 2 * args.steps + 1)
+    sample_base = rank * spp * (args.warmup + 3 * args.steps + 1)
 
     def render(k):
         rt.render(scene, spp, params, sample_base + k * spp, stream=sptr)
@@ -212,8 +216,6 @@ def run_xgb(args):
     for k in range(args.warmup):
         render(k)
     torch.cuda.synchronize()
-    scene.set_profiling(True)
-    stats = []
     with ClockSampler(local) as clocks:
         if dist:
             dist.barrier()
@@ -223,7 +225,6 @@ def run_xgb(args):
         e0.record(stream)
         for k in range(args.steps):
             render(args.warmup + k)
-            stats.append(scene.stats(stream=sptr))
         e1.record(stream)
         torch.cuda.synchronize()
         if dist:
@@ -236,8 +237,16 @@ def run_xgb(args):
     value = world * step_paths * args.steps / (ms_max / 1e3) / 1e6
     clk = clocks.summary()
 
-    # end to end through the C ABI: render call + film download to pinned host memory every step
+    # profiled pass (not timed above): CUDA events around every kernel on the
+    # render stream, plus BVH work counters, for the per-kernel roofline
+    scene.set_profiling(True)
+    stats = []
+    for k in range(max(1, min(args.steps, 5))):
+        render(args.warmup + args.steps + k)
+        stats.append(scene.stats(stream=sptr))
     scene.set_profiling(False)
+
+    # end to end through the C ABI: render call + film download to pinned host memory every step
     host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
     host_np = host.numpy()
     torch.cuda.synchronize()
@@ -245,7 +254,7 @@ def run_xgb(args):
         dist.barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        render(args.warmup + args.steps + k)
+        render(args.warmup + 2 * args.steps + k)
         rt.download(host_np, stream=sptr)
     t1 = time.perf_counter()
     e2e_s = torch.tensor([t1 - t0], dtype=torch.float64, device=f"cuda:{local}")
@@ -275,7 +284,8 @@ def run_xgb(args):
         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6.8 TB/s",
         "unit": "GB/s",
         "frac": (achieved / (hbm or 6800.0)) if achieved else None,
-        "traffic": None,
+        "traffic": EXTEND_DRAM_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
+        "traffic_source": "ncu dram__bytes_read+write per ray (profiles/extend_terrain_ncu_full.md) x rays per launch",
         "algorithmic_bytes_per_launch": EXTEND_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
         "avg_launch_ms": ext_ms / ext_launches,
         "bvh_l2_gbs": ((NODE_BYTES * agg["node_visits"] + TRI_BYTES * agg["tri_tests"]) / (ext_ms / 1e3) / 1e9
@@ -305,8 +315,8 @@ def run_xgb(args):
                    "queue_capacity": 1 << 21},
         "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC),
                 "d2h_bytes_per_step": W * H * 12},
-        "gpu_launches": agg["kernel_launches"],
-        "mrays_per_s": total_rays * world / (ms_max / 1e3) / 1e6,
+        "gpu_launches": agg["kernel_launches"] // len(stats) * args.steps,
+        "mrays_per_s": total_rays / len(stats) * args.steps * world / (ms_max / 1e3) / 1e6,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clk,

@@ -29,6 +29,8 @@ class CpuChecker:
         from . import build_ref
         if kind == "port":
             path, prefix = build_ref.build_oracle(), "xcpu_"
+        elif kind == "port_ulp":
+            path, prefix = build_ref.build_oracle_perturbed(), "xcpu_"
         elif kind == "reference":
             path, prefix = build_ref.build_ref(), "xref_"
             if path is None:
@@ -136,7 +138,7 @@ class CpuChecker:
 
     def trace(self, rays):
         """Closest hits of float32 [n, 7] rays (o, d, tMax) -> float32 [n, 5] (t, object, tri, -, -)."""
-        assert self.kind == "port"
+        assert self.kind.startswith("port")
         rays = np.ascontiguousarray(rays, dtype=np.float32)
         hits = np.zeros((rays.shape[0], 5), dtype=np.float32)
         r = self.lib.xcpu_trace(C.c_void_p(self.h), C.c_int(rays.shape[0]), rays.ctypes.data_as(C.POINTER(C.c_float)),
@@ -145,7 +147,7 @@ class CpuChecker:
         return hits
 
     def occluded(self, rays):
-        assert self.kind == "port"
+        assert self.kind.startswith("port")
         rays = np.ascontiguousarray(rays, dtype=np.float32)
         out = np.zeros(rays.shape[0], dtype=np.int32)
         r = self.lib.xcpu_occluded(C.c_void_p(self.h), C.c_int(rays.shape[0]), rays.ctypes.data_as(C.POINTER(C.c_float)),

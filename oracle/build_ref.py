@@ -40,6 +40,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 REF_SRC = os.path.join(REF_OUT, "src")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
+ORACLE_PERTURBED_SO = os.path.join(HERE, "liboracle_ulp.so")
 REF_SO = os.path.join(REF_OUT, "libxref.so")
 
 REFERENCE_ROOT = os.environ.get("XGB_REFERENCE_ROOT", "/root/reference")
@@ -90,8 +91,8 @@ def stage_reference(root: str = REFERENCE_ROOT) -> bool:
     return True
 
 
-def _compile(src: str, out: str, includes: list[str], std: str) -> None:
-    cmd = ["g++", f"-std={std}"] + CXXFLAGS + [f"-I{i}" for i in includes] + [src, "-o", out]
+def _compile(src: str, out: str, includes: list[str], std: str, defines: tuple = ()) -> None:
+    cmd = ["g++", f"-std={std}"] + CXXFLAGS + [f"-D{d}" for d in defines] + [f"-I{i}" for i in includes] + [src, "-o", out]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("compile failed: " + " ".join(cmd) + "\n" + res.stderr[-4000:])
@@ -103,6 +104,15 @@ def build_oracle(force: bool = False) -> str:
     if force or not os.path.exists(ORACLE_SO) or any(os.path.getmtime(d) > os.path.getmtime(ORACLE_SO) for d in deps):
         _compile(src, ORACLE_SO, [HERE], "c++17")
     return ORACLE_SO
+
+
+def build_oracle_perturbed(force: bool = False) -> str:
+    """The oracle with cosf / sinf / powf moved by one ulp: a sensitivity probe
+    used by tests to show how far last-ulp libm differences move an image."""
+    src = os.path.join(HERE, "xgb_cpu.cpp")
+    if force or not os.path.exists(ORACLE_PERTURBED_SO) or os.path.getmtime(src) > os.path.getmtime(ORACLE_PERTURBED_SO):
+        _compile(src, ORACLE_PERTURBED_SO, [HERE], "c++17", ("XGB_ORACLE_ULP_PERTURB",))
+    return ORACLE_PERTURBED_SO
 
 
 def build_ref(force: bool = False) -> str | None:

@@ -31,6 +31,19 @@
 
 namespace {
 
+#ifdef XGB_ORACLE_ULP_PERTURB
+// Sensitivity probe (tests only): every nonzero cosf / sinf / powf result moves one
+// ulp toward zero, the size of the difference between two libm implementations
+// (toward zero so that |cos| and |sin| never exceed 1).
+inline float towardZero(float r) { return r == 0.0f ? r : std::nextafter(r, 0.0f); }
+inline float perturbedCos(float x) { return towardZero(std::cos(x)); }
+inline float perturbedSin(float x) { return towardZero(std::sin(x)); }
+inline float perturbedPow(float x, float y) { return towardZero(std::pow(x, y)); }
+#define cosf perturbedCos
+#define sinf perturbedSin
+#define powf perturbedPow
+#endif
+
 const float kPi = (float)M_PI;  // Utils.h:32
 const float kInf = std::numeric_limits<float>::infinity();
 
@@ -1060,6 +1073,12 @@ Ray cameraRay(const Scene& sc, float fx, float fy) {
 }
 
 }  // namespace
+
+#ifdef XGB_ORACLE_ULP_PERTURB
+#undef cosf
+#undef sinf
+#undef powf
+#endif
 
 // ------------------------------------------------------------------ C API --
 extern "C" {

@@ -59,11 +59,27 @@ def test_terrain_ggx_latlong(ctx):
 
 
 @pytest.mark.parametrize("sky", ["none", "uniform", "probe", "latlong"])
-def test_material_zoo(ctx, sky):
-    desc = scenes.material_zoo(64, 64, 8, sky=sky)
+@pytest.mark.parametrize("only", [[], [1], [2], [3], [1, 2, 3]])
+def test_material_zoo(ctx, sky, only):
+    """Glossy, GlossyWithHighLight, SpecularReflection, SpecularFresnel under every sky."""
+    desc = scenes.material_zoo(64, 64, 8, sky=sky, only=only)
     _, _, err, close = _compare(ctx, desc, IntegratorParams())
     assert err <= TOL
-    assert close >= 0.95
+    assert close >= 0.98
+
+
+MFNM_TOL = 3e-2  # see test_oracle.py::test_mfnm_amplifies_last_ulp_differences
+
+
+@pytest.mark.parametrize("sky", ["none", "latlong"])
+def test_microfacet_normal_mapping(ctx, sky):
+    """MFNM with a normal map: a one-ulp libm perturbation of the oracle itself moves this
+    image by relMSE ~3e-3 (3% of pixels); the GPU must stay inside a small multiple of that
+    envelope and agree in mean to 1e-3."""
+    desc = scenes.material_zoo(64, 64, 8, sky=sky, only=[0])
+    gpu, cpu, err, _ = _compare(ctx, desc, IntegratorParams())
+    assert err <= MFNM_TOL
+    assert abs(gpu.mean() - cpu.mean()) <= 1e-3 * cpu.mean()
 
 
 def test_sample_ranges_add_up_and_match_oracle(ctx):

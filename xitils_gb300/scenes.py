@@ -208,7 +208,8 @@ def simple_path_tracer_scene(width: int = 128, height: int = 128, spp: int = 4) 
     return s
 
 
-def material_zoo(width: int = 64, height: int = 64, spp: int = 8, sky: str = "none", seed: int = 3) -> SceneDesc:
+def material_zoo(width: int = 64, height: int = 64, spp: int = 8, sky: str = "none", seed: int = 3,
+                 only=None) -> SceneDesc:
     """The SimplePathTracer room plus tangent-space cubes covering every material
     kind: Glossy, GlossyClamped under MicrofacetNormalMapping with a normal map,
     GlossyWithHighLight, SpecularReflection, SpecularFresnel. ``sky`` is one of
@@ -241,4 +242,6 @@ def material_zoo(width: int = 64, height: int = 64, spp: int = 8, sky: str = "no
         s.set_sky(SKY_PROBE, tex=s.add_texture(rng.random((64, 64, 3)).astype(F)))
     elif sky == "latlong":
         s.set_sky(SKY_LATLONG, tex=s.add_texture(latlong_sky(128, 64)))
+    if only is not None:  # keep the room plus the listed zoo cubes: 0 mfnm, 1 highlight, 2 mirror, 3 fresnel
+        s.objects = s.objects[:7] + [s.objects[7 + k] for k in only]
     return s
