@@ -180,6 +180,24 @@ typedef struct {
 /* Counters of the last xgb_render on this scene. Synchronises the stream. */
 xgb_status xgb_render_stats_get(xgb_scene* scene, xgb_render_stats* out, void* stream);
 
+/* No counterpart in the reference. The same render as xgb_render, for callers
+ * that cannot allocate GPU memory (a host that owns all device memory through
+ * its own pool, a frame loop that must not hit cudaMalloc's implicit device
+ * synchronisation, a plug-in given only a stream): the path queues, hit records,
+ * shadow queue and counters live in a fixed ~6 MB static __device__ array inside
+ * the library (held by every GPU that loads it), and the call makes no
+ * cudaMalloc, cudaFree or other allocation. At most XGB_NOALLOC_MAX_PATHS paths
+ * are in flight: params->queue_capacity above that returns XGB_INVALID_ARG
+ * (0 = the maximum); sample counts are not limited. Every call shares the array
+ * and re-initialises its counters, so calls whose GPU work overlaps (other
+ * streams or threads) race and must be serialised. The first call on a device
+ * looks up the array's address: make it before any stream capture. Errors are
+ * reported through the return code only (the context's error text is not
+ * touched). */
+#define XGB_NOALLOC_MAX_PATHS 32768
+xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_params* params, xgb_film* film,
+                              uint32_t spp_begin, uint32_t spp_count, void* stream);
+
 /* enable = 1: later xgb_render calls on this scene record CUDA events around
  * every kernel on the render stream and count BVH work (for profiling; adds a
  * few microseconds per wavefront iteration). */

@@ -94,6 +94,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_render": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
         "xgb_render_stats_get": [P, C.POINTER(RenderStatsC), P],
         "xgb_scene_set_profiling": [P, C.c_int],
+        "xgb_render_noalloc": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

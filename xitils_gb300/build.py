@@ -27,6 +27,7 @@ UNITS = {
     "bvh_build.cu": [],
     "trace.cu": [],
     "integrator.cu": ["-fmad=false"],
+    "noalloc.cu": [],
 }
 
 

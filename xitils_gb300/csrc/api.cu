@@ -993,3 +993,25 @@ xgb_status xgb_render_stats_get(xgb_scene* s, xgb_render_stats* out, void* strea
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------ internal accessors --
+// Read-only views used by other translation units of the library (no allocation).
+namespace xgb {
+bool sceneView(xgb_scene* s, SceneDev* sd, int* device, int* numSMs, cudaStream_t* stream, int* built) {
+    if (!s) return false;
+    *sd = s->sd;
+    *device = s->ctx->device;
+    *numSMs = s->ctx->numSMs;
+    *stream = s->ctx->stream;
+    *built = s->built ? 1 : 0;
+    return true;
+}
+bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp64) {
+    if (!f || !s || f->ctx != s->ctx) return false;
+    *d = f->d;
+    *w = f->w;
+    *h = f->h;
+    *fp64 = f->fp64;
+    return true;
+}
+}  // namespace xgb
