@@ -43,6 +43,8 @@ typedef struct xgb_film xgb_film;
 /* One context per GPU (and per host thread, or serialise calls on it). */
 xgb_status xgb_ctx_create(int device, xgb_ctx** out);
 xgb_status xgb_ctx_destroy(xgb_ctx* ctx);
+/* Waits for the work enqueued on stream (NULL = the context's own stream). */
+xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream);
 /* Last error message of this context ("" when none). Never NULL. */
 const char* xgb_get_last_error(const xgb_ctx* ctx);
 /* Library version string, e.g. "xgb 0.1 sm_103a". */
@@ -175,6 +177,7 @@ typedef struct {
        [0] plan, [1] generate, [2] extend (closest hit), [3] shade, [4] shadow (any hit) */
     double kernel_ms[5];
     uint64_t stage_launches[5];
+    uint64_t guide_train_steps; /* Adam steps of the learned proposal taken by the call */
 } xgb_render_stats;
 
 /* Counters of the last xgb_render on this scene. Synchronises the stream. */
@@ -197,6 +200,56 @@ xgb_status xgb_render_stats_get(xgb_scene* scene, xgb_render_stats* out, void* s
 #define XGB_NOALLOC_MAX_PATHS 32768
 xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_params* params, xgb_film* film,
                               uint32_t spp_begin, uint32_t spp_count, void* stream);
+
+/* ------------------------------------------------------ learned proposal */
+/* A 64-64-64-64-40 MLP (BF16 tensor-core kernels, FP32 accumulation, FP32 Adam
+ * master weights) mapping a shading point to an 8-lobe von Mises-Fisher mixture
+ * with the reference's lobe pdf and sampling (Include/Xitils/VonMisesFisherDistribution.h:
+ * pdf :205-211, sample :162-201). Inputs: 6-band sin/cos frequency encoding of the
+ * position normalised to the guide bounds, the position, the shading normal, wo.
+ * Outputs per lobe: m.xyz (mu = m/|m|), k (kappa = exp(clamp(k, -6, 8))), l
+ * (alpha = softmax(l)). No counterpart in the reference path tracer. */
+typedef struct xgb_guide xgb_guide;
+xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out);
+xgb_status xgb_guide_destroy(xgb_guide* guide);
+xgb_status xgb_guide_param_count(size_t* out);  /* 15,080 */
+/* Save / load: the FP32 master parameters (setting them resets Adam's moments). */
+xgb_status xgb_guide_get_params(xgb_guide* guide, float* host, size_t n);
+xgb_status xgb_guide_set_params(xgb_guide* guide, const float* host, size_t n);
+/* Gradients of the last xgb_guide_train_batch (or in-render training step). */
+xgb_status xgb_guide_get_grads(xgb_guide* guide, float* host, size_t n);
+/* Box the positions are normalised to (defaults to the scene bounds when rendering). */
+xgb_status xgb_guide_set_bounds(xgb_guide* guide, const float lo[3], const float hi[3]);
+/* Network outputs (n x 40) for host arrays of positions, normals and wo (n x 3 each). */
+xgb_status xgb_guide_infer(xgb_guide* guide, int n, const float* pos, const float* nrm, const float* wo, float* out);
+/* Draws one direction per point from the network's mixture with a PCG stream per
+ * index (seed), returning the directions (n x 3) and the mixture pdf (n). */
+xgb_status xgb_guide_sample(xgb_guide* guide, int n, const float* pos, const float* nrm, const float* wo, uint32_t seed,
+                            float* dirs, float* pdf);
+/* One Adam step (lr > 0; lr = 0 computes gradients only) on n <= 65536 samples of
+ * the loss sum_i -(w_i / sum w) log q(wi_i), w_i = radiance_i / pdf_i. *loss = the loss. */
+xgb_status xgb_guide_train_batch(xgb_guide* guide, int n, const float* pos, const float* nrm, const float* wo,
+                                 const float* wi, const float* pdf, const float* radiance, float lr, float* loss);
+/* In-render training (xgb_scene_set_guide with train = 1): a guided vertex of a
+ * camera path becomes a training record (at a rate that spreads about 2^20
+ * records over the call); when every path of the call has finished, a record's
+ * target is the incident radiance along its sampled direction (the path's
+ * later contributions divided by its throughput after the vertex), times the
+ * luminance of bsdfCos there when product_target = 1 (default). Records that
+ * carry radiance are pooled and consumed in Adam steps of batch_rows records
+ * (default 8192, a multiple of 64, at most 65536), at most max_steps_per_call
+ * (default 64) at the end of each call; a remainder smaller than a batch stays
+ * pooled for the next call. */
+xgb_status xgb_guide_set_training(xgb_guide* guide, int batch_rows, int max_steps_per_call, int product_target);
+/* Adam steps taken so far (explicit and in-render). */
+xgb_status xgb_guide_train_steps(xgb_guide* guide, uint64_t* out);
+/* Guided rendering: at Diffuse / Metal / Glossy vertices xgb_render samples the BSDF
+ * with probability bsdf_fraction and the learned mixture otherwise, weighting by
+ * the mixture density (one-sample MIS, unbiased at any network state); NEE's MIS
+ * uses the same density. train = 1 also trains the network online (see
+ * xgb_guide_set_training; standard integrator only; the call then holds 16
+ * bytes of device memory per camera path). guide = NULL turns guiding off. */
+xgb_status xgb_scene_set_guide(xgb_scene* scene, xgb_guide* guide, float bsdf_fraction, int train, float learning_rate);
 
 /* enable = 1: later xgb_render calls on this scene record CUDA events around
  * every kernel on the render stream and count BVH work (for profiling; adds a

@@ -41,7 +41,8 @@ class RenderStatsC(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("iterations", C.c_uint64), ("kernel_launches", C.c_uint64), ("node_visits", C.c_uint64),
                 ("tri_tests", C.c_uint64), ("error_flags", C.c_uint32), ("profiled", C.c_uint32),
-                ("kernel_ms", C.c_double * 5), ("stage_launches", C.c_uint64 * 5)]
+                ("kernel_ms", C.c_double * 5), ("stage_launches", C.c_uint64 * 5),
+                ("guide_train_steps", C.c_uint64)]
 
 
 _lib = None
@@ -60,6 +61,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     sig = {
         "xgb_ctx_create": [C.c_int, C.POINTER(P)],
         "xgb_ctx_destroy": [P],
+        "xgb_ctx_synchronize": [P, P],
         "xgb_texture_create": [P, C.c_int, C.c_int, C.c_int, FP, C.c_int, C.c_int, C.POINTER(P)],
         "xgb_texture_destroy": [P],
         "xgb_mesh_create": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(P)],
@@ -95,6 +97,19 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_render_stats_get": [P, C.POINTER(RenderStatsC), P],
         "xgb_scene_set_profiling": [P, C.c_int],
         "xgb_render_noalloc": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
+        "xgb_guide_create": [P, C.c_uint32, C.POINTER(P)],
+        "xgb_guide_destroy": [P],
+        "xgb_guide_param_count": [C.POINTER(C.c_size_t)],
+        "xgb_guide_get_params": [P, FP, C.c_size_t],
+        "xgb_guide_set_params": [P, FP, C.c_size_t],
+        "xgb_guide_get_grads": [P, FP, C.c_size_t],
+        "xgb_guide_set_bounds": [P, FP, FP],
+        "xgb_guide_infer": [P, C.c_int, FP, FP, FP, FP],
+        "xgb_guide_sample": [P, C.c_int, FP, FP, FP, C.c_uint32, FP, FP],
+        "xgb_guide_train_batch": [P, C.c_int, FP, FP, FP, FP, FP, FP, C.c_float, FP],
+        "xgb_guide_set_training": [P, C.c_int, C.c_int, C.c_int],
+        "xgb_guide_train_steps": [P, C.POINTER(C.c_uint64)],
+        "xgb_scene_set_guide": [P, P, C.c_float, C.c_int, C.c_float],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -136,6 +151,9 @@ class Context:
         if st != 0:
             msg = self.lib.xgb_get_last_error(self.h).decode()
             raise XgbError(st, f"{what}: {msg}")
+
+    def synchronize(self, stream=None):
+        self.check(self.lib.xgb_ctx_synchronize(self.h, stream), "synchronize")
 
     def close(self):
         if getattr(self, "h", None):
@@ -305,6 +323,11 @@ class Scene:
     def buildAccelerationStructure(self, stream=None):
         self.ctx.check(self.ctx.lib.xgb_scene_build(self.h, stream), "buildAccelerationStructure")
 
+    def setGuide(self, guide, bsdf_fraction: float = 0.5, train: bool = False, lr: float = 1e-3):
+        self.ctx.check(self.ctx.lib.xgb_scene_set_guide(self.h, guide.h if guide else None, C.c_float(bsdf_fraction),
+                                                        int(train), C.c_float(lr)), "setGuide")
+        self._guide = guide
+
     def set_profiling(self, enable: bool = True):
         self.ctx.check(self.ctx.lib.xgb_scene_set_profiling(self.h, int(enable)), "set_profiling")
 
@@ -347,6 +370,71 @@ class RenderTarget:
         f = C.c_int()
         self.ctx.check(self.ctx.lib.xgb_film_device_pointer(self.h, C.byref(p), C.byref(f)), "device_pointer")
         return p.value, bool(f.value)
+
+
+class Guide:
+    """The learned directional proposal (xgb_guide_*): an MLP predicting an
+    8-lobe vMF mixture, trained with Adam on BF16 tensor cores."""
+
+    N_OUT = 40
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        self.h = P()
+        ctx.check(ctx.lib.xgb_guide_create(ctx.h, seed, C.byref(self.h)), "Guide")
+        n = C.c_size_t()
+        ctx.lib.xgb_guide_param_count(C.byref(n))
+        self.n_params = n.value
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        self.ctx.check(self.ctx.lib.xgb_guide_get_params(self.h, _fp(out), out.size), "get_params")
+        return out
+
+    def set_params(self, p):
+        p = _f32(p, self.n_params)
+        self.ctx.check(self.ctx.lib.xgb_guide_set_params(self.h, _fp(p), p.size), "set_params")
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        self.ctx.check(self.ctx.lib.xgb_guide_get_grads(self.h, _fp(out), out.size), "get_grads")
+        return out
+
+    def set_bounds(self, lo, hi):
+        self.ctx.check(self.ctx.lib.xgb_guide_set_bounds(self.h, _fp(_f32(lo, 3)), _fp(_f32(hi, 3))), "set_bounds")
+
+    def infer(self, pos, nrm, wo) -> np.ndarray:
+        pos, nrm, wo = (_f32(a).reshape(-1, 3) for a in (pos, nrm, wo))
+        out = np.empty((pos.shape[0], self.N_OUT), np.float32)
+        self.ctx.check(self.ctx.lib.xgb_guide_infer(self.h, pos.shape[0], _fp(pos), _fp(nrm), _fp(wo), _fp(out)),
+                       "infer")
+        return out
+
+    def sample(self, pos, nrm, wo, seed: int = 0):
+        pos, nrm, wo = (_f32(a).reshape(-1, 3) for a in (pos, nrm, wo))
+        n = pos.shape[0]
+        dirs = np.empty((n, 3), np.float32)
+        pdf = np.empty(n, np.float32)
+        self.ctx.check(self.ctx.lib.xgb_guide_sample(self.h, n, _fp(pos), _fp(nrm), _fp(wo), seed, _fp(dirs), _fp(pdf)),
+                       "sample")
+        return dirs, pdf
+
+    def set_training(self, batch_rows: int = 8192, max_steps_per_call: int = 64, product: bool = True):
+        self.ctx.check(self.ctx.lib.xgb_guide_set_training(self.h, batch_rows, max_steps_per_call, int(product)),
+                       "set_training")
+
+    def steps(self) -> int:
+        n = C.c_uint64()
+        self.ctx.check(self.ctx.lib.xgb_guide_train_steps(self.h, C.byref(n)), "train_steps")
+        return n.value
+
+    def train_batch(self, pos, nrm, wo, wi, pdf, radiance, lr: float) -> float:
+        arrs = [_f32(a).reshape(-1, 3) for a in (pos, nrm, wo, wi)]
+        pdf, radiance = _f32(pdf), _f32(radiance)
+        loss = np.zeros(1, np.float32)
+        self.ctx.check(self.ctx.lib.xgb_guide_train_batch(self.h, arrs[0].shape[0], *[_fp(a) for a in arrs], _fp(pdf),
+                                                          _fp(radiance), C.c_float(lr), _fp(loss)), "train_batch")
+        return float(loss[0])
 
 
 class GpuSceneBuilder:

@@ -28,6 +28,7 @@ UNITS = {
     "trace.cu": [],
     "integrator.cu": ["-fmad=false"],
     "noalloc.cu": [],
+    "guide.cu": [],
 }
 
 

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/xgb.h"
+#include "guide_kernels.h"
 #include "xgb_kernels.h"
 
 using namespace xgb;
@@ -131,6 +132,21 @@ struct xgb_film {
     void* d = nullptr;
 };
 
+struct xgb_guide {
+    xgb_ctx* ctx;
+    GuideDevice g;
+    GuideBounds bounds;
+    bool hasBounds = false;
+    std::vector<void*> allocations;
+    GuideRecord* arena = nullptr;           // training records of one render call
+    int arenaCap = 0;
+    unsigned int* recCount = nullptr;       // [0] arena count, [3] pool count
+    GuideRecord* batchRec = nullptr;        // device staging for xgb_guide_train_batch
+    unsigned int* hostPoolCount = nullptr;  // pinned copy of the pool count
+    int maxStepsPerCall = 64;
+    int product = 1;                        // target: radiance x bsdfCos (1) or radiance (0)
+};
+
 struct SceneObject {
     const xgb_mesh* mesh;
     const xgb_material* material;
@@ -164,6 +180,16 @@ struct xgb_scene {
     xgb_render_stats last{};
     bool profiling = false;
     std::vector<cudaEvent_t> events;  // profiling: 6 per wavefront iteration
+    float boundsLo[3] = {0, 0, 0}, boundsHi[3] = {1, 1, 1};  // world bounds of the built scene
+    xgb_guide* guide = nullptr;
+    float bsdfFrac = 0.5f;
+    int guideTrain = 0;
+    float guideLr = 1e-3f;
+    float4* mix = nullptr;  // per-path mixtures (capacity x 10 float4)
+    unsigned int mixCapacity = 0;
+    float4* pathAcc = nullptr;  // guide training: per-path contributions of a call
+    unsigned long long pathAccCapacity = 0;
+    double vertsPerPath = 4.0;  // extension rays per path of the last call (sizes the record rate)
 };
 
 static xgb_status fail(xgb_ctx* ctx, xgb_status st, const std::string& msg) {
@@ -211,6 +237,12 @@ xgb_status xgb_ctx_destroy(xgb_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
+    return XGB_OK;
+}
+
+xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream) {
+    if (!ctx) return XGB_INVALID_ARG;
+    XGB_CUDA(ctx, cudaStreamSynchronize(pick(ctx, stream)));
     return XGB_OK;
 }
 
@@ -497,6 +529,8 @@ xgb_status xgb_scene_destroy(xgb_scene* s) {
     cudaStreamSynchronize(s->ctx->stream);
     freeSceneDevice(s);
     freeBuffers(s);
+    dfree(s->mix);
+    dfree(s->pathAcc);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     dfree(s->ctrl);
     if (s->ctrlHost) cudaFreeHost(s->ctrlHost);
@@ -721,6 +755,10 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
         }
     }
 
+    Box sceneBox;
+    for (const Box& b : boxes) sceneBox.add(b);
+    for (int k = 0; k < 3; ++k) { s->boundsLo[k] = sceneBox.lo[k]; s->boundsHi[k] = sceneBox.hi[k]; }
+
     // top-level hierarchy
     std::vector<Node2> tlas;
     int tlasRootIsLeaf = 0;
@@ -741,7 +779,12 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     };
     SceneDev& sd = s->sd;
     MeshDev* dMeshes; Instance* dInst; Node2* dTlas; Material* dMat; TextureDev* dTex = nullptr; LightDev* dLights = nullptr;
-    float4* dLN = nullptr; float* dLP = nullptr;
+    float4* dLN = nullptr; float* dLP = nullptr; float4* dBox = nullptr;
+    std::vector<float4> instBox(2 * inst.size());
+    for (size_t i = 0; i < inst.size(); ++i) {
+        instBox[2 * i] = make_float4(boxes[i].lo[0], boxes[i].lo[1], boxes[i].lo[2], 0.0f);
+        instBox[2 * i + 1] = make_float4(boxes[i].hi[0], boxes[i].hi[1], boxes[i].hi[2], 0.0f);
+    }
     XGB_CUDA(ctx, up(&dMeshes, md));
     XGB_CUDA(ctx, up(&dInst, inst));
     XGB_CUDA(ctx, up(&dTlas, tlas));
@@ -750,11 +793,13 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     XGB_CUDA(ctx, up(&dLights, lights));
     XGB_CUDA(ctx, up(&dLN, lightNormal));
     XGB_CUDA(ctx, up(&dLP, lightPdf));
+    XGB_CUDA(ctx, up(&dBox, instBox));
     sd.meshes = dMeshes;
     sd.instances = dInst;
     sd.tlas = dTlas;
     sd.nInstances = (int)inst.size();
     sd.tlasRootIsLeaf = tlasRootIsLeaf;
+    sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;
     sd.lights = dLights;
@@ -840,10 +885,10 @@ void xgb_integrator_params_default(xgb_integrator_params* p) {
 static xgb_status ensureBuffers(xgb_scene* s, unsigned int cap) {
     if (s->rb.capacity >= cap && s->rb.block) return XGB_OK;
     freeBuffers(s);
-    size_t pathBytes = (size_t)cap * (16 * 3 + 8);
+    size_t pathBytes = (size_t)cap * (16 * 3 + 8 + 4 + 4);
     size_t hitBytes = (size_t)cap * (16 + 4);
-    size_t shadowBytes = (size_t)cap * (16 * 3 + 8);
-    size_t total = 2 * pathBytes + hitBytes + shadowBytes + 64 * 16;
+    size_t shadowBytes = (size_t)cap * (16 * 3 + 8 + 4);
+    size_t total = 2 * pathBytes + hitBytes + shadowBytes + 64 * 256;
     void* block = nullptr;
     cudaError_t e = cudaMalloc(&block, total);
     if (e != cudaSuccess) return fail(s->ctx, XGB_OOM, "render: cannot allocate path queues");
@@ -854,6 +899,8 @@ static xgb_status ensureBuffers(xgb_scene* s, unsigned int cap) {
         s->rb.q[k].d = (float4*)take(16 * (size_t)cap);
         s->rb.q[k].thr = (float4*)take(16 * (size_t)cap);
         s->rb.q[k].rng = (uint2*)take(8 * (size_t)cap);
+        s->rb.q[k].grec = (int*)take(4 * (size_t)cap);
+        s->rb.q[k].pid = (unsigned int*)take(4 * (size_t)cap);
     }
     s->rb.hits.h = (float4*)take(16 * (size_t)cap);
     s->rb.hits.inst = (int*)take(4 * (size_t)cap);
@@ -861,6 +908,7 @@ static xgb_status ensureBuffers(xgb_scene* s, unsigned int cap) {
     s->rb.shadow.d = (float4*)take(16 * (size_t)cap);
     s->rb.shadow.c = (float4*)take(16 * (size_t)cap);
     s->rb.shadow.rng = (uint2*)take(8 * (size_t)cap);
+    s->rb.shadow.pid = (unsigned int*)take(4 * (size_t)cap);
     s->rb.block = block;
     s->rb.capacity = cap;
     return XGB_OK;
@@ -894,7 +942,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     if (bs) return bs;
     cap = s->rb.capacity;
 
-    RenderParams rp;
+    RenderParams rp{};
     rp.width = film->w; rp.height = film->h;
     rp.sppBegin = spp_begin;
     rp.seed = P.seed;
@@ -905,6 +953,54 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.capacity = cap;
     rp.filmFp64 = film->fp64;
     rp.film = film->d;
+    rp.guided = 0;
+    rp.train = 0;
+    rp.bsdfFrac = s->bsdfFrac;
+    xgb_guide* gd = s->guide;
+    GuideBounds gb;
+    if (gd) {
+        if (s->mixCapacity < cap) {
+            dfree(s->mix);
+            s->mix = nullptr;
+            s->mixCapacity = 0;
+            if (cudaMalloc((void**)&s->mix, sizeof(float4) * 10 * (size_t)cap) != cudaSuccess)
+                return fail(ctx, XGB_OOM, "xgb_render: cannot allocate guiding mixtures");
+            s->mixCapacity = cap;
+        }
+        rp.guided = 1;
+        rp.mix = s->mix;
+        rp.train = s->guideTrain && P.integrator == XGB_INTEGRATOR_STANDARD;
+        if (rp.train) {
+            if (total > 0xFFFFFFF0ull)
+                return fail(ctx, XGB_INVALID_ARG, "xgb_render: guide training needs fewer than 2^32 paths per call");
+            if (s->pathAccCapacity < total) {
+                dfree(s->pathAcc);
+                s->pathAcc = nullptr;
+                s->pathAccCapacity = 0;
+                if (cudaMalloc((void**)&s->pathAcc, sizeof(float4) * (size_t)total) != cudaSuccess)
+                    return fail(ctx, XGB_OOM, "xgb_render: cannot allocate guide training accumulators");
+                s->pathAccCapacity = total;
+            }
+            rp.pathAcc = s->pathAcc;
+            rp.arena = gd->arena;
+            rp.arenaCount = gd->recCount;
+            rp.arenaCap = gd->arenaCap;
+            // spread the records over the whole call rather than its first vertices
+            double expected = (double)total * std::max(1.0, s->vertsPerPath);
+            rp.recordProb = (float)std::min(1.0, (double)gd->arenaCap / expected);
+        }
+        if (gd->hasBounds) {
+            gb = gd->bounds;
+        } else {
+            for (int k = 0; k < 3; ++k) {
+                gb.lo[k] = s->boundsLo[k];
+                float e = s->boundsHi[k] - s->boundsLo[k];
+                gb.invExtent[k] = e > 0 ? 1.0f / e : 1.0f;
+            }
+        }
+        if (rp.train) XGB_CUDA(ctx, cudaMemsetAsync(gd->recCount, 0, sizeof(unsigned int), st));
+    }
+    uint64_t guideSteps = 0;
 
     Ctrl init;
     std::memset(&init, 0, sizeof(init));
@@ -937,6 +1033,10 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
             launchGenerate(s->sd, rp, X, s->ctrl, gShade, st);
             if (prof) cudaEventRecord(ev[2], st);
             launchExtend(s->sd, X, s->rb.hits, s->ctrl, gTrace, prof, st);
+            if (gd) {
+                guideInferPaths(s->sd, gd->g, gb, X, s->rb.hits, s->ctrl, s->mix, gShade, st);
+                ++launches;
+            }
             if (prof) cudaEventRecord(ev[3], st);
             launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, gShade, st);
             if (prof) cudaEventRecord(ev[4], st);
@@ -960,7 +1060,21 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
         if (c.nextPath >= c.totalPaths && c.nOut == 0) break;
         if (guard > (1 << 22)) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: wavefront did not drain");
     }
+    if (gd && rp.train) {
+        // every path of the call has finished: records take their incident
+        // radiance, those that carry some join the pool, and the pool is
+        // consumed in fixed-size Adam steps
+        guideFinalizeRecords(gd->arena, gd->recCount, gd->arenaCap, s->pathAcc, gd->product, st);
+        guideCollect(gd->g, gd->arena, gd->recCount, gd->arenaCap, st);
+        XGB_CUDA(ctx, cudaMemcpyAsync(gd->hostPoolCount, gd->g.poolCount, 4, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(ctx, cudaStreamSynchronize(st));
+        int n = guidePoolTrain(gd->g, *gd->hostPoolCount, gb, s->guideLr, gd->maxStepsPerCall, st);
+        guideSteps += (uint64_t)n;
+        launches += 2 + 17 * (uint64_t)n + 1;
+        XGB_CUDA(ctx, cudaGetLastError());
+    }
     const Ctrl& c = *s->ctrlHost;
+    if (c.pathsDone > 0) s->vertsPerPath = (double)c.extensionRays / (double)c.pathsDone;
     s->last.paths = c.pathsDone;
     s->last.extension_rays = c.extensionRays;
     s->last.shadow_rays = c.shadowRays;
@@ -969,6 +1083,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     s->last.kernel_launches = launches;
     s->last.node_visits = c.nodeVisits;
     s->last.tri_tests = c.triTests;
+    s->last.guide_train_steps = guideSteps;
     s->last.profiled = prof ? 1 : 0;
     for (int j = 0; j < 5; ++j) {
         s->last.kernel_ms[j] = stageMs[j];
@@ -1015,3 +1130,269 @@ bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp
     return true;
 }
 }  // namespace xgb
+
+// ------------------------------------------------------------ guiding MLP --
+namespace {
+// splitmix64-based uniform in [-1, 1) for deterministic initialisation.
+float initUniform(uint64_t& state) {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)((z >> 40) * (1.0 / 8388608.0)) - 1.0f;
+}
+}  // namespace
+
+extern "C" {
+
+xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
+    if (!ctx || !out) return XGB_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    auto* gd = new xgb_guide();
+    gd->ctx = ctx;
+    GuideDevice& g = gd->g;
+    g.maxRows = 65536;
+    g.step = 0;
+    const int R = g.maxRows;
+    auto alloc = [&](size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, bytes);
+        gd->allocations.push_back(p);
+        return p;
+    };
+    bool ok = true;
+    auto A = [&](size_t bytes) { void* p = alloc(bytes); ok = ok && p; return p; };
+    g.params = (float*)A(4 * kGuideParams);
+    g.grads = (float*)A(4 * kGuideParams);
+    g.m = (float*)A(4 * kGuideParams);
+    g.v = (float*)A(4 * kGuideParams);
+    for (int l = 0; l < 3; ++l) {
+        g.w.W[l] = (__nv_bfloat16*)A(2 * 64 * 64);
+        g.w.WT[l] = (__nv_bfloat16*)A(2 * 64 * 64);
+        g.w.bias[l] = (float*)A(4 * 64);
+    }
+    g.w.W[3] = (__nv_bfloat16*)A(2 * kGuideOutPad * 64);
+    g.w.WT[3] = (__nv_bfloat16*)A(2 * 64 * kGuideOutPad);
+    g.w.bias[3] = (float*)A(4 * kGuideOutPad);
+    for (int l = 0; l < 4; ++l) g.scratch.X[l] = (__nv_bfloat16*)A(2 * (size_t)R * 64);
+    g.scratch.dirw = (float4*)A(16 * (size_t)R);
+    g.scratch.Y = (float*)A(4 * (size_t)R * kGuideOutPad);
+    g.scratch.dY3 = (__nv_bfloat16*)A(2 * (size_t)R * kGuideOutPad);
+    for (int l = 0; l < 3; ++l) g.scratch.dZ[l] = (__nv_bfloat16*)A(2 * (size_t)R * 64);
+    g.scratch.dW = (float*)A(4 * (3 * 64 * 64 + kGuideOutPad * 64 + 256));
+    g.scratch.scalars = (float*)A(16);
+    gd->arenaCap = 1 << 20;
+    gd->arena = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)gd->arenaCap);
+    gd->recCount = (unsigned int*)A(4 * 4);
+    gd->batchRec = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)R);
+    g.poolCap = 8 * R;
+    g.batch = 8192;
+    g.pool = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)g.poolCap);
+    g.poolCount = gd->recCount + 3;
+    if (ok && cudaMallocHost((void**)&gd->hostPoolCount, 4) != cudaSuccess) {
+        gd->hostPoolCount = nullptr;
+        ok = false;
+    }
+    if (!ok) {
+        if (gd->hostPoolCount) cudaFreeHost(gd->hostPoolCount);
+        for (void* p : gd->allocations) dfree(p);
+        delete gd;
+        return fail(ctx, XGB_OOM, "xgb_guide_create: out of device memory");
+    }
+    // He-uniform hidden layers, zero biases; a small output layer whose biases
+    // spread 8 broad lobes (kappa = 1, equal weights) over the sphere.
+    std::vector<float> p(kGuideParams, 0.0f);
+    uint64_t st = 0x1234567ull ^ ((uint64_t)seed << 20);
+    const float hs = std::sqrt(6.0f / 64.0f);
+    for (int i = kGuideW0; i < kGuideB0; ++i) p[i] = hs * initUniform(st);
+    for (int i = kGuideW1; i < kGuideB1; ++i) p[i] = hs * initUniform(st);
+    for (int i = kGuideW2; i < kGuideB2; ++i) p[i] = hs * initUniform(st);
+    for (int i = kGuideW3; i < kGuideB3; ++i) p[i] = 0.01f * initUniform(st);
+    const float dirs[8][3] = {{1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1}, {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}};
+    for (int j = 0; j < kGuideLobes; ++j) {
+        p[kGuideB3 + 5 * j + 0] = dirs[j][0];
+        p[kGuideB3 + 5 * j + 1] = dirs[j][1];
+        p[kGuideB3 + 5 * j + 2] = dirs[j][2];
+        p[kGuideB3 + 5 * j + 3] = 0.0f;
+        p[kGuideB3 + 5 * j + 4] = 0.0f;
+    }
+    cudaMemcpy(g.params, p.data(), 4 * kGuideParams, cudaMemcpyHostToDevice);
+    guideRefresh(g, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        for (void* q : gd->allocations) dfree(q);
+        delete gd;
+        return fail(ctx, XGB_CUDA_ERROR, "xgb_guide_create: initialisation failed");
+    }
+    *out = gd;
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_destroy(xgb_guide* gd) {
+    if (!gd) return XGB_INVALID_ARG;
+    cudaSetDevice(gd->ctx->device);
+    cudaStreamSynchronize(gd->ctx->stream);
+    for (void* p : gd->allocations) dfree(p);
+    if (gd->hostPoolCount) cudaFreeHost(gd->hostPoolCount);
+    delete gd;
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_param_count(size_t* out) {
+    if (!out) return XGB_INVALID_ARG;
+    *out = kGuideParams;
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_get_params(xgb_guide* gd, float* host, size_t n) {
+    if (!gd || !host || n != (size_t)kGuideParams) return XGB_INVALID_ARG;
+    XGB_CUDA(gd->ctx, cudaStreamSynchronize(gd->ctx->stream));
+    XGB_CUDA(gd->ctx, cudaMemcpy(host, gd->g.params, 4 * n, cudaMemcpyDeviceToHost));
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_set_params(xgb_guide* gd, const float* host, size_t n) {
+    if (!gd || !host || n != (size_t)kGuideParams) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = gd->ctx;
+    XGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    XGB_CUDA(ctx, cudaMemcpy(gd->g.params, host, 4 * n, cudaMemcpyHostToDevice));
+    XGB_CUDA(ctx, cudaMemset(gd->g.m, 0, 4 * n));
+    XGB_CUDA(ctx, cudaMemset(gd->g.v, 0, 4 * n));
+    gd->g.step = 0;
+    guideRefresh(gd->g, ctx->stream);
+    XGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_get_grads(xgb_guide* gd, float* host, size_t n) {
+    if (!gd || !host || n != (size_t)kGuideParams) return XGB_INVALID_ARG;
+    XGB_CUDA(gd->ctx, cudaStreamSynchronize(gd->ctx->stream));
+    XGB_CUDA(gd->ctx, cudaMemcpy(host, gd->g.grads, 4 * n, cudaMemcpyDeviceToHost));
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_set_bounds(xgb_guide* gd, const float lo[3], const float hi[3]) {
+    if (!gd || !lo || !hi) return XGB_INVALID_ARG;
+    for (int k = 0; k < 3; ++k) {
+        if (!(hi[k] > lo[k])) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_set_bounds: need hi > lo");
+        gd->bounds.lo[k] = lo[k];
+        gd->bounds.invExtent[k] = 1.0f / (hi[k] - lo[k]);
+    }
+    gd->hasBounds = true;
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_infer(xgb_guide* gd, int n, const float* pos, const float* nrm, const float* wo, float* out) {
+    if (!gd || n < 0 || (n > 0 && (!pos || !nrm || !wo || !out))) return XGB_INVALID_ARG;
+    if (!gd->hasBounds) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_infer: call xgb_guide_set_bounds first");
+    xgb_ctx* ctx = gd->ctx;
+    cudaStream_t st = ctx->stream;
+    const int R = gd->g.maxRows;
+    float* dIn = nullptr;
+    XGB_CUDA(ctx, cudaMalloc((void**)&dIn, 4 * 9 * (size_t)R));
+    std::vector<float> y((size_t)R * kGuideOutPad);
+    for (int b = 0; b < n; b += R) {
+        int cnt = std::min(R, n - b);
+        int rows = ((cnt + 63) / 64) * 64;
+        cudaMemcpyAsync(dIn, pos + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dIn + 3 * R, nrm + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dIn + 6 * R, wo + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
+        guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, cnt, rows, gd->bounds, gd->g.scratch.X[0], st);
+        guideInferRows(gd->g, gd->g.scratch.X[0], rows, gd->g.scratch.Y, st);
+        cudaMemcpyAsync(y.data(), gd->g.scratch.Y, 4 * (size_t)rows * kGuideOutPad, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) {
+            cudaFree(dIn);
+            return fail(ctx, XGB_CUDA_ERROR, "xgb_guide_infer failed");
+        }
+        for (int r = 0; r < cnt; ++r)
+            std::memcpy(out + (size_t)(b + r) * kGuideOut, y.data() + (size_t)r * kGuideOutPad, 4 * kGuideOut);
+    }
+    cudaFree(dIn);
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_sample(xgb_guide* gd, int n, const float* pos, const float* nrm, const float* wo, uint32_t seed,
+                            float* dirs, float* pdf) {
+    if (!gd || n < 0 || (n > 0 && (!pos || !nrm || !wo || !dirs || !pdf))) return XGB_INVALID_ARG;
+    if (n > gd->g.maxRows) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_sample: at most 65536 points");
+    if (!gd->hasBounds) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_sample: call xgb_guide_set_bounds first");
+    if (n == 0) return XGB_OK;
+    xgb_ctx* ctx = gd->ctx;
+    cudaStream_t st = ctx->stream;
+    const int R = gd->g.maxRows;
+    float* dIn = nullptr;
+    XGB_CUDA(ctx, cudaMalloc((void**)&dIn, 4 * 13 * (size_t)R));
+    int rows = ((n + 63) / 64) * 64;
+    cudaMemcpyAsync(dIn, pos, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dIn + 3 * R, nrm, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dIn + 6 * R, wo, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
+    guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, n, rows, gd->bounds, gd->g.scratch.X[0], st);
+    guideInferRows(gd->g, gd->g.scratch.X[0], rows, gd->g.scratch.Y, st);
+    guideSampleRows(gd->g.scratch.Y, n, seed, dIn + 9 * R, dIn + 12 * R, st);
+    cudaMemcpyAsync(dirs, dIn + 9 * R, 12 * (size_t)n, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(pdf, dIn + 12 * R, 4 * (size_t)n, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(dIn);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "xgb_guide_sample");
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_train_batch(xgb_guide* gd, int n, const float* pos, const float* nrm, const float* wo,
+                                 const float* wi, const float* pdf, const float* radiance, float lr, float* loss) {
+    if (!gd || n <= 0 || !pos || !nrm || !wo || !wi || !pdf || !radiance || lr < 0) return XGB_INVALID_ARG;
+    if (n > gd->g.maxRows) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_train_batch: at most 65536 samples");
+    if (!gd->hasBounds) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_train_batch: call xgb_guide_set_bounds first");
+    xgb_ctx* ctx = gd->ctx;
+    cudaStream_t st = ctx->stream;
+    std::vector<GuideRecord> rec(n);
+    for (int i = 0; i < n; ++i) {
+        rec[i].p = make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        rec[i].n = make_float3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+        rec[i].wo = make_float3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        rec[i].wi = make_float3(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]);
+        rec[i].pdf = pdf[i];
+        rec[i].radiance = radiance[i];
+    }
+    XGB_CUDA(ctx, cudaMemcpyAsync(gd->batchRec, rec.data(), sizeof(GuideRecord) * n, cudaMemcpyHostToDevice, st));
+    guideTrainStep(gd->g, gd->batchRec, n, gd->bounds, lr, st);
+    float sc[2];
+    XGB_CUDA(ctx, cudaMemcpyAsync(sc, gd->g.scratch.scalars, 8, cudaMemcpyDeviceToHost, st));
+    XGB_CUDA(ctx, cudaStreamSynchronize(st));
+    XGB_CUDA(ctx, cudaGetLastError());
+    if (loss) *loss = sc[1];
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_set_training(xgb_guide* gd, int batch_rows, int max_steps_per_call, int product_target) {
+    if (!gd) return XGB_INVALID_ARG;
+    if (batch_rows < 64 || batch_rows > gd->g.maxRows || (batch_rows & 63))
+        return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_set_training: batch_rows must be a multiple of 64 in [64, 65536]");
+    if (max_steps_per_call < 1) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_set_training: max_steps_per_call >= 1");
+    XGB_CUDA(gd->ctx, cudaStreamSynchronize(gd->ctx->stream));
+    gd->g.batch = batch_rows;
+    gd->maxStepsPerCall = max_steps_per_call;
+    gd->product = product_target ? 1 : 0;
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_train_steps(xgb_guide* gd, uint64_t* out) {
+    if (!gd || !out) return XGB_INVALID_ARG;
+    *out = (uint64_t)gd->g.step;
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_set_guide(xgb_scene* s, xgb_guide* gd, float bsdf_fraction, int train, float learning_rate) {
+    if (!s) return XGB_INVALID_ARG;
+    if (gd && gd->ctx != s->ctx) return fail(s->ctx, XGB_INVALID_ARG, "xgb_scene_set_guide: guide of another context");
+    if (gd && !(bsdf_fraction > 0.0f && bsdf_fraction < 1.0f))
+        return fail(s->ctx, XGB_INVALID_ARG, "xgb_scene_set_guide: bsdf_fraction must be in (0, 1)");
+    if (gd && train && !(learning_rate > 0.0f)) return fail(s->ctx, XGB_INVALID_ARG, "xgb_scene_set_guide: learning rate");
+    s->guide = gd;
+    s->bsdfFrac = bsdf_fraction;
+    s->guideTrain = (gd && train) ? 1 : 0;
+    s->guideLr = learning_rate;
+    return XGB_OK;
+}
+
+}  // extern "C"

@@ -12,6 +12,7 @@
 // Russian-roulette draw, the BSDF sample, the light sample (object, triangle,
 // barycentrics) and, only when the light is visible, a stochastic bsdfCos.
 // This translation unit is compiled with -fmad=false.
+#include "guide.cuh"
 #include "materials.cuh"
 #include "xgb_kernels.h"
 
@@ -74,41 +75,12 @@ __global__ void __launch_bounds__(kShadeBlock) k_generate(SceneDev sc, RenderPar
         q.d[s] = make_float4(d.x, d.y, d.z, __int_as_float(len | (FLAG_PRIMARY << 16)));
         q.thr[s] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float((int)pix));
         q.rng[s] = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
+        if (rp.train) {
+            q.grec[s] = -1;
+            q.pid[s] = (unsigned int)g;
+            rp.pathAcc[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
     }
-}
-
-// SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).
-__device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instance& in, int prim, float b0, float b1,
-                                               V3 dWorld) {
-    const MeshDev& m = sc.meshes[in.mesh];
-    int i0 = m.idx[3 * prim], i1 = m.idx[3 * prim + 1], i2 = m.idx[3 * prim + 2];
-    V3 p0 = v3(m.pos[i0]), p1 = v3(m.pos[i1]), p2 = v3(m.pos[i2]);
-    V3 dObj = in.identity ? dWorld : xformVector(in.matInv, dWorld);
-    Surface s;
-    s.uv = m.uv ? lerp3(m.uv[i0], m.uv[i1], m.uv[i2], b0, b1) : make_float2(0.0f, 0.0f);
-    s.p = lerp3(p0, p1, p2, b0, b1);
-    s.wo = normalize(-dObj);
-    s.n = m.nrm ? normalize(lerp3(v3(m.nrm[i0]), v3(m.nrm[i1]), v3(m.nrm[i2]), b0, b1)) : v3(m.gnrm[prim]);
-    s.sn = s.n;
-    if (m.tan) {
-        s.stan = normalize(lerp3(v3(m.tan[i0]), v3(m.tan[i1]), v3(m.tan[i2]), b0, b1));
-        s.sbit = normalize(lerp3(v3(m.bit[i0]), v3(m.bit[i1]), v3(m.bit[i2]), b0, b1));
-    } else {
-        s.stan = V3();
-        s.sbit = V3();
-    }
-    s.sn = faceForward(s.sn, s.wo);
-    // object -> world (an identity matrix product is exact, its normalize is not skipped)
-    if (!in.identity) s.p = xformPoint(in.mat, s.p);
-    s.n = in.identity ? normalize(s.n) : xformNormal(in.mat, s.n);
-    s.wo = in.identity ? normalize(s.wo) : xformNormal(in.mat, s.wo);
-    const Material& mat = sc.materials[in.material];
-    if (mat.normalmap >= 0) {
-        V3 nm = texLookup(sc.textures[mat.normalmap], s.uv.x, s.uv.y) * 2.0f - V3(1.0f);
-        s.sn = normalize(nm.z * s.sn + nm.x * s.stan + nm.y * s.sbit);
-    }
-    s.sn = in.identity ? normalize(s.sn) : xformNormal(in.mat, s.sn);
-    return s;
 }
 
 struct LightSampleD {
@@ -160,11 +132,40 @@ struct ShadeOut {
     // continuing path
     float4 o, d, thr;
     uint2 rng;
+    int grec;
     // shadow ray
     float4 so, sd, sc;
     uint2 srng;
     bool stochastic;
 };
+
+// Whether a guided vertex becomes a training record: a hash of (path, depth),
+// so that the decision draws nothing from the path's own random stream.
+__device__ __forceinline__ bool keepRecord(unsigned int pid, int len, float prob) {
+    if (prob >= 1.0f) return true;
+    uint64_t z = splitmix64(((uint64_t)pid << 8) ^ (uint64_t)(len & 0xFF) ^ 0x9E3779B97F4A7C15ull);
+    return (float)(z >> 40) * (1.0f / 16777216.0f) < prob;
+}
+
+__device__ __forceinline__ float luminance(V3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+// Materials the learned proposal may sample: non-delta BSDFs whose bsdfCos and
+// getPDF are deterministic.
+__device__ __forceinline__ bool guidable(int kind) {
+    return kind == MAT_DIFFUSE || kind == MAT_METAL || kind == MAT_GLOSSY || kind == MAT_GLOSSY_CLAMPED ||
+           kind == MAT_GLOSSY_HIGHLIGHT;
+}
+
+__device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
+    for (int j = 0; j < kGuideLobes; ++j) {
+        float4 a = m[j];
+        mx.lobe[j].mu = V3(a.x, a.y, a.z);
+        mx.lobe[j].kappa = a.w;
+    }
+    float4 a0 = m[8], a1 = m[9];
+    mx.lobe[0].alpha = a0.x; mx.lobe[1].alpha = a0.y; mx.lobe[2].alpha = a0.z; mx.lobe[3].alpha = a0.w;
+    mx.lobe[4].alpha = a1.x; mx.lobe[5].alpha = a1.y; mx.lobe[6].alpha = a1.z; mx.lobe[7].alpha = a1.w;
+}
 
 __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams rp, PathQueue in, HitQueue hq,
                                                        PathQueue out, ShadowQueue sq, Ctrl* ctrl) {
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
         bool cont = false, shadow = false, done = false;
         ShadeOut r;
         r.stochastic = false;
+        r.grec = -1;
         if (i < n) {
             float4 o4 = in.o[i], d4 = in.d[i], t4 = in.thr[i];
             uint2 rs = in.rng[i];
@@ -191,15 +193,31 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
             const float pdfPrev = o4.w;
             V3 dir(d4.x, d4.y, d4.z);
             V3 thr(t4.x, t4.y, t4.z);
+            // guide training: the record of the vertex this ray left takes the
+            // path's accumulated contribution now, before this vertex adds any
+            const unsigned int pid = rp.train ? in.pid[i] : 0u;
+            if (rp.train) {
+                const int prevRec = in.grec[i];
+                if (prevRec >= 0) {
+                    float4 a = rp.pathAcc[pid];
+                    rp.arena[prevRec].snap = make_float3(a.x, a.y, a.z);
+                }
+            }
+            V3 acc(0.0f);  // this vertex's contributions (training accumulator)
+            auto contribute = [&](V3 c) {
+                filmAddS(rp, pix, c);
+                if (rp.train) acc = acc + c;
+            };
             Pcg rng;
             rng.state = ((uint64_t)rs.y << 32) | rs.x;
             rng.inc = ((uint64_t)(unsigned int)pix << 1) | 1u;
             if (prim < 0) {
                 // Miss: the sky, with no MIS (PathTracer.h:133-136, 192-197).
                 if (sc.skyKind != SKY_NONE) {
-                    V3 L = thr * skyRadiance(sc, dir);
+                    V3 Ls = skyRadiance(sc, dir);
+                    V3 L = thr * Ls;
                     if (naive) L = clampPositive(L);  // PathTracer.h:96
-                    filmAddS(rp, pix, L);
+                    contribute(L);
                 }
                 done = true;
             } else {
@@ -232,7 +250,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                         done = true;
                     }
                 } else if (flags & FLAG_PRIMARY) {
-                    if (emissive) filmAddS(rp, pix, thr * emission(mat, -dir, s.n));  // PathTracer.h:143-145
+                    if (emissive) contribute(thr * emission(mat, -dir, s.n));  // PathTracer.h:143-145
                 } else if (emissive) {
                     // BSDF-sampled hit on an emitter (PathTracer.h:171-190).
                     float mis;
@@ -245,7 +263,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                     } else {
                         mis = 1.0f;
                     }
-                    if (mis > 0.0f) filmAddS(rp, pix, thr * mis * emission(mat, -dir, s.n));
+                    if (mis > 0.0f) contribute(thr * mis * emission(mat, -dir, s.n));
                 }
                 // An emitter's evalAndSample is zero: the path ends there (its NEE
                 // contribution is multiplied by Emission::bsdfCos() == 0).
@@ -266,7 +284,35 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                     } else {
                         V3 wi;
                         float pdf = pdfPrev;  // left untouched by materials that do not set it
-                        V3 f = evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                        V3 f;
+                        const bool guidedHere = rp.guided && guidable(mat.kind);
+                        VmfMixture mx;
+                        float fcos = 0.0f;  // luminance of bsdfCos(wi) at a guided vertex
+                        if (!guidedHere) {
+                            f = evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                        } else {
+                            // One-sample MIS of the BSDF and the learned vMF mixture (balance
+                            // heuristic): pdf = frac p_bsdf + (1 - frac) p_vmf; unbiased at any
+                            // network state because the BSDF keeps support everywhere.
+                            loadMixture(rp.mix + (size_t)i * 10, mx);
+                            const float frac = rp.bsdfFrac;
+                            if (rng.randf() < frac) {
+                                float pb = 0.0f;
+                                V3 e = evalAndSample(sc, mat, s, rng, &wi, &pb);
+                                float pm = frac * pb + (1.0f - frac) * mixturePdf(mx, wi);
+                                f = (pb > 0.0f && pm > 0.0f) ? e * (pb / pm) : V3(0.0f);
+                                fcos = luminance(e) * pb;
+                                pdf = pm;
+                            } else {
+                                wi = mixtureSample(mx, rng);
+                                float pb = getPDF(sc, mat, s, wi);
+                                float pm = frac * pb + (1.0f - frac) * mixturePdf(mx, wi);
+                                V3 bc = bsdfCos(sc, mat, s, rng, wi);
+                                f = pm > 0.0f ? bc / pm : V3(0.0f);
+                                fcos = luminance(bc);
+                                pdf = pm;
+                            }
+                        }
                         if (!naive && sc.nLights > 0) {  // PathTracer.h:202-233
                             LightSampleD ls = sampleLight(sc, rng);
                             V3 toL = ls.p - s.p;
@@ -279,6 +325,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                                 float mis;
                                 if (pdf >= 0.0f) {
                                     float pb = getPDF(sc, mat, s, sd);
+                                    if (guidedHere) pb = rp.bsdfFrac * pb + (1.0f - rp.bsdfFrac) * mixturePdf(mx, sd);
                                     float cosLight = fabsf(dot(-sd, ls.sn));
                                     pb *= cosLight / distSq;
                                     mis = (ls.pdf * ls.pdf) / ((pb * pb) + (ls.pdf * ls.pdf));
@@ -289,7 +336,8 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                                     float G = fabsf(dot(-sd, ls.sn)) / distSq;
                                     Pcg spec = rng;  // bsdfCos draws only if the light is visible
                                     V3 bc = bsdfCos(sc, mat, s, spec, sd);
-                                    V3 c = thr * mis * bc * emission(sc.materials[ls.material], -sd, ls.n) * G / ls.pdf;
+                                    V3 Le = emission(sc.materials[ls.material], -sd, ls.n);
+                                    V3 c = thr * mis * bc * Le * G / ls.pdf;
                                     r.so = make_float4(so.x, so.y, so.z, stMax);
                                     r.sd = make_float4(sd.x, sd.y, sd.z, __int_as_float(pix));
                                     r.sc = make_float4(c.x, c.y, c.z, 0.0f);
@@ -307,11 +355,35 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                             r.thr = make_float4(thrNext.x, thrNext.y, thrNext.z, __int_as_float(pix));
                             r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
                             cont = true;
+                            if (rp.train && guidedHere && pdf > 0.0f && keepRecord(pid, len, rp.recordProb)) {
+                                unsigned int slot = atomicAdd(rp.arenaCount, 1u);
+                                if (slot < (unsigned int)rp.arenaCap) {
+                                    GuideRecord g;
+                                    g.p = make_float3(s.p.x, s.p.y, s.p.z);
+                                    g.pdf = pdf;
+                                    g.n = make_float3(s.sn.x, s.sn.y, s.sn.z);
+                                    g.fcos = fcos;
+                                    g.wo = make_float3(s.wo.x, s.wo.y, s.wo.z);
+                                    g.pid = pid;
+                                    g.wi = make_float3(wi.x, wi.y, wi.z);
+                                    g.radiance = 0.0f;
+                                    g.snap = make_float3(__int_as_float(0x7fc00000), 0.0f, 0.0f);
+                                    g.pad0 = 0.0f;
+                                    g.thr = make_float3(thrNext.x, thrNext.y, thrNext.z);
+                                    g.pad1 = 0.0f;
+                                    rp.arena[slot] = g;
+                                    r.grec = (int)slot;
+                                }
+                            }
                         } else {
                             done = true;
                         }
                     }
                 }
+            }
+            if (rp.train && !isZero(acc)) {
+                float4 a = rp.pathAcc[pid];
+                rp.pathAcc[pid] = make_float4(a.x + acc.x, a.y + acc.y, a.z + acc.z, a.w);
             }
         }
         // compacted writes: continuing paths, then shadow rays (which may point at them)
@@ -325,6 +397,10 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
             out.d[slot] = r.d;
             out.thr[slot] = r.thr;
             out.rng[slot] = r.rng;
+            if (rp.train) {
+                out.grec[slot] = r.grec;
+                out.pid[slot] = in.pid[i];
+            }
         }
         unsigned int ms = __ballot_sync(kFull, shadow);
         unsigned int os = 0;
@@ -337,6 +413,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
             r.sc.w = __int_as_float((r.stochastic && cont) ? (int)slot : -1);
             sq.c[ss] = r.sc;
             sq.rng[ss] = r.srng;
+            if (rp.train) sq.pid[ss] = in.pid[i];
         }
         unsigned int md = __ballot_sync(kFull, done);
         if (lane == 0 && md) atomicAdd(&ctrl->pathsDone, (unsigned long long)__popc(md));

@@ -398,4 +398,38 @@ __device__ __forceinline__ V3 albedoOf(const SceneDev& sc, const Material& m, co
     }
 }
 
+// SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).
+__device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instance& in, int prim, float b0, float b1,
+                                               V3 dWorld) {
+    const MeshDev& m = sc.meshes[in.mesh];
+    int i0 = m.idx[3 * prim], i1 = m.idx[3 * prim + 1], i2 = m.idx[3 * prim + 2];
+    V3 p0 = v3(m.pos[i0]), p1 = v3(m.pos[i1]), p2 = v3(m.pos[i2]);
+    V3 dObj = in.identity ? dWorld : xformVector(in.matInv, dWorld);
+    Surface s;
+    s.uv = m.uv ? lerp3(m.uv[i0], m.uv[i1], m.uv[i2], b0, b1) : make_float2(0.0f, 0.0f);
+    s.p = lerp3(p0, p1, p2, b0, b1);
+    s.wo = normalize(-dObj);
+    s.n = m.nrm ? normalize(lerp3(v3(m.nrm[i0]), v3(m.nrm[i1]), v3(m.nrm[i2]), b0, b1)) : v3(m.gnrm[prim]);
+    s.sn = s.n;
+    if (m.tan) {
+        s.stan = normalize(lerp3(v3(m.tan[i0]), v3(m.tan[i1]), v3(m.tan[i2]), b0, b1));
+        s.sbit = normalize(lerp3(v3(m.bit[i0]), v3(m.bit[i1]), v3(m.bit[i2]), b0, b1));
+    } else {
+        s.stan = V3();
+        s.sbit = V3();
+    }
+    s.sn = faceForward(s.sn, s.wo);
+    // object -> world (an identity matrix product is exact, its normalize is not skipped)
+    if (!in.identity) s.p = xformPoint(in.mat, s.p);
+    s.n = in.identity ? normalize(s.n) : xformNormal(in.mat, s.n);
+    s.wo = in.identity ? normalize(s.wo) : xformNormal(in.mat, s.wo);
+    const Material& mat = sc.materials[in.material];
+    if (mat.normalmap >= 0) {
+        V3 nm = texLookup(sc.textures[mat.normalmap], s.uv.x, s.uv.y) * 2.0f - V3(1.0f);
+        s.sn = normalize(nm.z * s.sn + nm.x * s.stan + nm.y * s.sbit);
+    }
+    s.sn = in.identity ? normalize(s.sn) : xformNormal(in.mat, s.sn);
+    return s;
+}
+
 }  // namespace xgb

@@ -123,7 +123,7 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     sq.rng = (uint2*)take(kU2);
     Ctrl* ctrl = (Ctrl*)take(up(sizeof(Ctrl)));
 
-    RenderParams rp;
+    RenderParams rp{};  // learned-proposal fields stay off (0 / nullptr)
     rp.width = W; rp.height = H;
     rp.sppBegin = spp_begin;
     rp.seed = P.seed;

@@ -20,6 +20,12 @@ __device__ __forceinline__ void filmAdd(const RenderParams& rp, int pix, V3 c) {
     }
 }
 
+// Guide training: a visible light's contribution also goes to its path's accumulator.
+__device__ __forceinline__ void creditPath(const RenderParams& rp, unsigned int pid, float4 c) {
+    float4 a = rp.pathAcc[pid];
+    rp.pathAcc[pid] = make_float4(a.x + c.x, a.y + c.y, a.z + c.z, a.w);
+}
+
 constexpr int kTraceBlock = 128;
 
 template <bool COUNT>
@@ -79,47 +85,55 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(SceneDev sc, RenderParam
                 // stream only because the light was visible (PathTracer.h:209-227):
                 // commit the stream position it left.
                 if (target >= 0) out.rng[target] = s.rng[i];
+                if (rp.train) creditPath(rp, s.pid[i], c);
             }
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctrl->shadowRays, (unsigned long long)n);
 }
 
-// ---- single-mesh scenes ------------------------------------------------------
-// When the scene is one instance, traversal runs as a persistent per-lane state
-// machine in the style of Aila & Laine ("Understanding the Efficiency of Ray
-// Traversal on GPUs", HPG 2009): a lane whose ray is finished fetches the next
-// one at once (one atomicAdd per group of lanes), inner nodes and leaves are
-// processed in separate inner loops, and the first leaf a lane reaches is
-// postponed until every lane of the warp holds one, so that the warp tests
-// triangles together. Results are identical to traceScene: the same slab and
-// watertight tests, the same closest-hit acceptance.
+// ---- scenes of a few instances ------------------------------------------------
+// With at most kFlatInstances instances the top level is a short list: a lane
+// walks the instances in order (those whose world box the ray still reaches
+// within tMax) and traverses each mesh BVH as a persistent per-lane state machine
+// in the style of Aila & Laine ("Understanding the Efficiency of Ray Traversal
+// on GPUs", HPG 2009): a lane whose ray is finished fetches the next one at once
+// (one atomicAdd per group of lanes), inner nodes and leaves are processed in
+// separate inner loops, and the first leaf a lane reaches is postponed until
+// every lane of the warp holds one, so that the warp tests triangles together.
+// Results are those of traceScene: the same slab and watertight tests and the
+// same closest-hit acceptance (tMax shrinks across instances).
 constexpr int kSentinel = 0x7FFFFFFF;
+constexpr int kFlatInstances = 16;
 
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
-                                                              ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+__global__ void __launch_bounds__(kTraceBlock) k_trace_flat(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
+                                                            ShadowQueue s, PathQueue out, Ctrl* ctrl) {
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
     unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
-    const Instance& in = sc.instances[0];
-    const MeshDev m = sc.meshes[in.mesh];
-    const bool identity = in.identity != 0;
+    const int nInst = sc.nInstances;
     const int lane = threadIdx.x & 31;
     const unsigned int ltMask = (1u << lane) - 1u;
     int stack[kStackDepth];
     int sp = 0;
     int nodeAddr = kSentinel, leafAddr = 0;
+    int inst = nInst;  // instance being traversed; nInst = ray finished
     unsigned int ray = 0;
+    V3 wo(0.f, 0.f, 0.f), wd(0.f, 0.f, 1.f);
     WRay r;
+    const Node2* nodes = nullptr;
+    const TriV* tris = nullptr;
     float tMax = 0.0f;
     TraceHit hit;
     hit.prim = -1;
+    hit.inst = -1;
     hit.t = 0.0f;
     hit.b0 = hit.b1 = 0.0f;
     bool occluded = false;
+    bool fetch = true;
     WorkCount wc;
     for (int guard = 0;; ++guard) {
-        if (nodeAddr == kSentinel) {
+        if (fetch) {
             // lanes without a ray fetch the next ones together
             const unsigned int act = __activemask();
             const int leader = __ffs(act) - 1;
@@ -131,25 +145,58 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, Rende
             float4 o4, d4;
             if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
             else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
-            V3 o(o4.x, o4.y, o4.z), d(d4.x, d4.y, d4.z);
-            if (!identity) {
-                o = xformPointRn(in.matInv, o);
-                d = xformVectorRn(in.matInv, d);
-            }
-            r = makeWRay(o, d);
+            wo = V3(o4.x, o4.y, o4.z);
+            wd = V3(d4.x, d4.y, d4.z);
             hit.prim = -1;
+            hit.inst = -1;
             hit.t = tMax;
             occluded = false;
-            sp = 0;
             guard = 0;
+            inst = -1;
+            nodeAddr = kSentinel;
+            leafAddr = 0;
+            fetch = false;
+        }
+        if (nodeAddr == kSentinel && leafAddr >= 0) {
+            // next instance whose world box the ray still reaches
+            WRay wr = makeWRay(wo, wd);
+            for (++inst; inst < nInst; ++inst) {
+                float4 lo = __ldg(&sc.instBox[2 * inst]), hi = __ldg(&sc.instBox[2 * inst + 1]);
+                float tn;
+                if (slab(wr, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tMax, tn)) break;
+            }
+            if (ANY && occluded) inst = nInst;
+            if (inst >= nInst) {  // ray finished
+                if (ANY) {
+                    if (!occluded) {
+                        float4 cc = s.c[ray];
+                        filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
+                        int target = __float_as_int(cc.w);
+                        if (target >= 0) out.rng[target] = s.rng[ray];
+                        if (rp.train) creditPath(rp, s.pid[ray], cc);
+                    }
+                } else {
+                    h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
+                    h.inst[ray] = hit.inst;
+                }
+                fetch = true;
+                continue;
+            }
+            const Instance& in = sc.instances[inst];
+            const MeshDev& m = sc.meshes[in.mesh];
+            nodes = m.nodes;
+            tris = m.tris;
+            if (in.identity) r = wr;
+            else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
+            sp = 0;
             if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > kMaxVisits) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
+        if (guard > kMaxVisits) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; inst = nInst; }
         bool searching = true;
         while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
             if (COUNT) wc.nodes++;
-            const Node2* nd = m.nodes + nodeAddr;
+            const Node2* nd = nodes + nodeAddr;
             float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
             int4 dd = __ldg(&nd->d);
             float t0, t1;
@@ -179,7 +226,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, Rende
             int first = leafFirst(leafAddr), cnt = leafCount(leafAddr);
             if (COUNT) wc.tris += cnt;
             for (int k = 0; k < cnt; ++k) {
-                const TriV* tv = m.tris + first + k;
+                const TriV* tv = tris + first + k;
                 float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
                 float t, b0, b1;
                 if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
@@ -187,24 +234,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, Rende
                     if (ANY) { occluded = true; break; }
                     hit.t = t; hit.b0 = b0; hit.b1 = b1;
                     hit.prim = __float_as_int(p0.w);
+                    hit.inst = inst;
                 }
             }
-            if (ANY && occluded) { leafAddr = 0; nodeAddr = kSentinel; break; }
+            if (ANY && occluded) { leafAddr = 0; nodeAddr = kSentinel; sp = 0; break; }
             leafAddr = nodeAddr;  // another leaf was postponed: take it next
             if (nodeAddr < 0) nodeAddr = sp > 0 ? stack[--sp] : kSentinel;
-        }
-        if (nodeAddr == kSentinel && leafAddr >= 0) {  // ray finished
-            if (ANY) {
-                if (!occluded) {
-                    float4 cc = s.c[ray];
-                    filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
-                    int target = __float_as_int(cc.w);
-                    if (target >= 0) out.rng[target] = s.rng[ray];
-                }
-            } else {
-                h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
-                h.inst[ray] = hit.prim >= 0 ? 0 : -1;
-            }
         }
     }
     if (COUNT) {
@@ -235,9 +270,9 @@ int shadowBlocksPerSM() {
 
 void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int grid, bool count, cudaStream_t s) {
     RenderParams none{};
-    if (sc.nInstances == 1) {
-        if (count) k_trace_single<false, true><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-        else k_trace_single<false, false><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    if (sc.nInstances <= kFlatInstances) {
+        if (count) k_trace_flat<false, true><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else k_trace_flat<false, false><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         return;
     }
     if (count) k_extend<true><<<grid, kTraceBlock, 0, s>>>(sc, q, h, ctrl);
@@ -245,8 +280,8 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int g
 }
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int grid,
                   cudaStream_t s) {
-    if (sc.nInstances == 1) {
-        k_trace_single<true, false><<<grid, kTraceBlock, 0, s>>>(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    if (sc.nInstances <= kFlatInstances) {
+        k_trace_flat<true, false><<<grid, kTraceBlock, 0, s>>>(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
         return;
     }
     k_shadow<<<grid, kTraceBlock, 0, s>>>(sc, rp, sq, out, ctrl);

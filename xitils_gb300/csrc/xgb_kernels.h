@@ -51,20 +51,43 @@ struct Ctrl {
 enum ErrorBits : unsigned int { ERR_STACK = 1u, ERR_QUEUE = 2u, ERR_LOOP = 4u };
 
 struct PathQueue {
-    float4* o;    // o.xyz, w = pdf of the BSDF sample that produced this ray (-1: specular)
-    float4* d;    // d.xyz, w = bits: pathLength | flags << 16
-    float4* thr;  // throughput.xyz, w = bits: pixel index
-    uint2* rng;   // PCG state
+    float4* o;          // o.xyz, w = pdf of the BSDF sample that produced this ray (-1: specular)
+    float4* d;          // d.xyz, w = bits: pathLength | flags << 16
+    float4* thr;        // throughput.xyz, w = bits: pixel index
+    uint2* rng;         // PCG state
+    int* grec;          // guide training: record of the vertex this ray left (-1: none)
+    unsigned int* pid;  // guide training: index of the path within the render call
 };
+
+// One training sample of the guiding network: a guided vertex, the direction
+// sampled there and, once the path has finished, the incident radiance found
+// along it: (contributions of the later vertices) / (throughput after this vertex).
+struct __align__(16) GuideRecord {
+    float3 p;
+    float pdf;        // density wi was sampled with (mixture of BSDF and network)
+    float3 n;
+    float fcos;       // luminance of bsdfCos(wi) (product target)
+    float3 wo;
+    unsigned int pid; // path index within the render call
+    float3 wi;
+    float radiance;   // training target (luminance), filled in when the call ends
+    float3 snap;      // the path's accumulated contribution before the next vertex (NaN: none)
+    float pad0;
+    float3 thr;       // path throughput after this vertex
+    float pad1;
+};
+static_assert(sizeof(GuideRecord) == 96, "GuideRecord size");
+
 struct HitQueue {
     float4* h;    // t, b0, b1, bits(prim); prim = -1 on a miss
     int* inst;
 };
 struct ShadowQueue {
-    float4* o;    // o.xyz, tMax
-    float4* d;    // d.xyz, bits(pixel)
-    float4* c;    // contribution rgb, bits(output-queue index of the path or -1)
-    uint2* rng;   // PCG state after a stochastic bsdfCos (committed if visible)
+    float4* o;          // o.xyz, tMax
+    float4* d;          // d.xyz, bits(pixel)
+    float4* c;          // contribution rgb, bits(output-queue index of the path or -1)
+    uint2* rng;         // PCG state after a stochastic bsdfCos (committed if visible)
+    unsigned int* pid;  // guide training: path credited with the contribution
 };
 
 enum PathFlags : int { FLAG_PRIMARY = 1, FLAG_STOCHASTIC_NEE = 2 };
@@ -80,6 +103,16 @@ struct RenderParams {
     unsigned int capacity;
     int filmFp64;
     void* film;  // float4* or double4*
+    // learned proposal (0 / nullptr when off)
+    int guided;
+    int train;
+    float bsdfFrac;           // one-sample MIS: probability of sampling the BSDF
+    const float4* mix;        // per input path: 8 x (mu, kappa) then 8 weights
+    GuideRecord* arena;       // training records of this call
+    unsigned int* arenaCount; // may run past arenaCap (writers drop)
+    int arenaCap;
+    float recordProb;         // probability that a guided vertex becomes a record
+    float4* pathAcc;          // per path of the call: contributions so far (rgb)
 };
 
 void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s);

@@ -115,6 +115,7 @@ struct SceneDev {
     const Node2* tlas;
     int nInstances;
     int tlasRootIsLeaf;
+    const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;
     const LightDev* lights;

@@ -1,0 +1,101 @@
+"""Equal-time comparison of neural-guided and plain NEE+MIS rendering.
+
+Protocol: a converged reference image is rendered with the plain path tracer
+(FP64 film), then each method renders progressive passes for the same GPU time
+budget T. The guided run trains the network online during the first
+``train_fraction`` of T and renders with the frozen network for the rest; every
+pass of both runs is kept (guided passes are unbiased at any network state,
+because the BSDF remains a sampling strategy of the one-sample MIS). The score
+is relMSE = mean((I - R)^2 / (R^2 + 1e-2)) against the reference.
+"""
+from __future__ import annotations
+
+import time
+from typing import Optional
+
+import numpy as np
+
+from . import api
+from .scene import IntegratorParams, SceneDesc
+
+
+def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
+    img = np.asarray(img, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
+
+
+def render_reference(ctx: api.Context, builder: api.GpuSceneBuilder, desc: SceneDesc, spp: int,
+                     chunk: int = 256, seed_offset: int = 1 << 20) -> np.ndarray:
+    """Plain path tracer, FP64 film, sample indices disjoint from the compared runs."""
+    rt = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
+    builder.scene.setGuide(None)
+    done = 0
+    while done < spp:
+        n = min(chunk, spp - done)
+        rt.render(builder.scene, n, desc.params, seed_offset + done)
+        done += n
+    return rt.download() / spp
+
+
+def _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass=None, sample_base=0):
+    rt = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
+    spp = 0
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    while True:
+        elapsed = time.perf_counter() - t0
+        if elapsed >= time_s:
+            break
+        if on_pass:
+            on_pass(elapsed)
+        rt.render(builder.scene, pass_spp, params, sample_base + spp)
+        spp += pass_spp
+    img = rt.download() / max(spp, 1)
+    return img, spp, time.perf_counter() - t0
+
+
+def _warm_up(ctx, builder, desc, params, pass_spp):
+    """One untimed pass (buffer allocation, first launches) before an arm is timed."""
+    rt = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
+    rt.render(builder.scene, pass_spp, params, 1 << 30)
+    rt.download()
+
+
+def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0, train_fraction: float = 0.25,
+                          reference_spp: int = 16384, pass_spp: int = 1, bsdf_fraction: float = 0.5,
+                          lr: float = 1e-3, reference: Optional[np.ndarray] = None, seed: int = 0,
+                          batch_rows: int = 8192, builder=None) -> dict:
+    """Both arms are warmed up by one untimed pass; the guided arm's clock
+    includes its network inference and every training step."""
+    builder = builder if builder is not None else api.load_scene(ctx, desc)
+    params = desc.params
+    ref = reference if reference is not None else render_reference(ctx, builder, desc, reference_spp)
+    builder.scene.setGuide(None)
+    _warm_up(ctx, builder, desc, params, pass_spp)
+    plain, plain_spp, plain_t = _timed_passes(ctx, builder, desc, time_s, pass_spp, params)
+    warm = api.Guide(ctx, seed=seed + 1)  # allocations and first launches of the guided path, then discarded
+    builder.scene.setGuide(warm, bsdf_fraction, train=True, lr=lr)
+    _warm_up(ctx, builder, desc, params, pass_spp)
+    guide = api.Guide(ctx, seed=seed)
+    guide.set_training(batch_rows)
+    state = {"training": True}
+    builder.scene.setGuide(guide, bsdf_fraction, train=True, lr=lr)
+
+    def on_pass(elapsed):
+        if state["training"] and elapsed >= train_fraction * time_s:
+            builder.scene.setGuide(guide, bsdf_fraction, train=False)
+            state["training"] = False
+
+    guided, guided_spp, guided_t = _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass)
+    builder.scene.setGuide(None)
+    rp, rg = relmse(plain, ref), relmse(guided, ref)
+    return {
+        "time_s": time_s, "train_fraction": train_fraction, "bsdf_fraction": bsdf_fraction,
+        "reference_spp": reference_spp if reference is None else None,
+        "plain": {"spp": plain_spp, "seconds": plain_t, "relmse": rp, "mse": float(np.mean((plain - ref) ** 2))},
+        "guided": {"spp": guided_spp, "seconds": guided_t, "relmse": rg, "mse": float(np.mean((guided - ref) ** 2)),
+                   "train_steps": guide.steps()},
+        "relmse_ratio_plain_over_guided": rp / rg if rg > 0 else None,
+        "images": (plain, guided, ref),
+    }

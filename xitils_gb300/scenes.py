@@ -245,3 +245,59 @@ def material_zoo(width: int = 64, height: int = 64, spp: int = 8, sky: str = "no
     if only is not None:  # keep the room plus the listed zoo cubes: 0 mfnm, 1 highlight, 2 mirror, 3 fresnel
         s.objects = s.objects[:7] + [s.objects[7 + k] for k in only]
     return s
+
+
+def box_mesh(centers, sizes, angles):
+    """Axis-aligned boxes (the reference Cube's corner order and triangles) scaled
+    per box, rotated about y and translated, merged into one vertex/index array."""
+    cpos, cidx = unit_cube_mesh()
+    n = len(centers)
+    c, s = np.cos(angles), np.sin(angles)
+    local = cpos[None, :, :] * sizes[:, None, :]
+    x = local[:, :, 0] * c[:, None] + local[:, :, 2] * s[:, None]
+    z = -local[:, :, 0] * s[:, None] + local[:, :, 2] * c[:, None]
+    pos = np.stack([x, local[:, :, 1], z], axis=2) + centers[:, None, :]
+    idx = (cidx[None, :] + 8 * np.arange(n)[:, None]).reshape(-1)
+    return pos.reshape(-1, 3).astype(F), idx.astype(np.int32)
+
+
+def occluded_room(width: int = 1024, height: int = 1024, spp: int = 4, n_boxes: int = 16667, seed: int = 11,
+                  max_depth: int = 0) -> SceneDesc:
+    """Occluded-light interior: a 10 x 4 x 10 room whose only light, a 0.5 x 0.5
+    quad of radiance 200, sits behind a partition wall at x = 8.5 and shines into
+    the room through a 1.0 x 0.2 slit; ~200k triangles of seeded random boxes
+    (edge lengths U[0.1, 1]) resting on the floor clutter the main room, so paths
+    are indirect-dominated."""
+    s = SceneDesc(name="occluded_room", width=width, height=height, spp=spp,
+                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed))
+    rng = np.random.default_rng(seed)
+    grey = s.diffuse([0.7, 0.7, 0.7])
+    light = s.emission([200.0, 200.0, 200.0])
+    # room shell (quads facing inward; Diffuse shading is two-sided anyway)
+    X, Y, Z, WX = 10.0, 4.0, 10.0, 8.5
+    shell = [quad([0, 0, 0], [X, 0, 0], [X, 0, Z], [0, 0, Z]), quad([0, Y, 0], [0, Y, Z], [X, Y, Z], [X, Y, 0]),
+             quad([0, 0, 0], [0, 0, Z], [0, Y, Z], [0, Y, 0]), quad([X, 0, 0], [X, Y, 0], [X, Y, Z], [X, 0, Z]),
+             quad([0, 0, 0], [0, Y, 0], [X, Y, 0], [X, 0, 0]), quad([0, 0, Z], [X, 0, Z], [X, Y, Z], [0, Y, Z])]
+    # partition wall at x = WX with a slit y in [1.9, 2.1], z in [4.5, 5.5]: four panels
+    gy0, gy1, gz0, gz1 = 1.9, 2.1, 4.5, 5.5
+    panels = [quad([WX, 0, 0], [WX, gy0, 0], [WX, gy0, Z], [WX, 0, Z]),
+              quad([WX, gy1, 0], [WX, Y, 0], [WX, Y, Z], [WX, gy1, Z]),
+              quad([WX, gy0, 0], [WX, gy1, 0], [WX, gy1, gz0], [WX, gy0, gz0]),
+              quad([WX, gy0, gz1], [WX, gy1, gz1], [WX, gy1, Z], [WX, gy0, Z])]
+    sizes = rng.uniform(0.1, 1.0, (n_boxes, 3))
+    centers = np.stack([rng.uniform(0.3, WX - 0.3, n_boxes), np.zeros(n_boxes), rng.uniform(0.3, Z - 0.3, n_boxes)], 1)
+    centers[:, 1] = sizes[:, 1] / 2  # resting on the floor: a clutter layer at most 1 m deep
+    bpos, bidx = box_mesh(centers, sizes, rng.uniform(0, np.pi, n_boxes))
+    parts = shell + panels + [(bpos, bidx)]
+    pos_all, idx_all, off = [], [], 0
+    for pos, idx in parts:
+        pos_all.append(np.asarray(pos, F))
+        idx_all.append(np.asarray(idx, np.int32) + off)
+        off += len(pos)
+    s.add_object(s.add_mesh(np.concatenate(pos_all), np.concatenate(idx_all)), grey)
+    lz, ly, h = 5.0, 2.0, 0.25
+    lx = 9.9  # light quad facing -x (toward the slit)
+    pos, idx = quad([lx, ly - h, lz - h], [lx, ly - h, lz + h], [lx, ly + h, lz + h], [lx, ly + h, lz - h])
+    s.add_object(s.add_mesh(pos, idx), light)
+    s.set_camera(look_at((1.2, 2.6, 1.0), (6.0, 1.6, 6.5), (0, 1, 0)), 70.0 * math.pi / 180.0, height / width)
+    return s
