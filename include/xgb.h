@@ -137,6 +137,29 @@ xgb_status xgb_film_clear(xgb_film* film, void* stream);
 xgb_status xgb_film_download(xgb_film* film, float* host, int pixel_stride_bytes, void* stream);
 /* Device address of the film (float4 or double4 per pixel, w unused). */
 xgb_status xgb_film_device_pointer(xgb_film* film, void** out, int* is_fp64);
+/* DenoisableRenderTarget (RenderTarget.h:131-145): xgb_render also sums the
+ * first hit's Material::getAlbedo and geometric normal (PathTracer.h:76-80,
+ * 138-139; zero for a camera ray that misses) into two more planes of the
+ * film's element type. Cleared by xgb_film_clear. */
+#define XGB_AOV_ALBEDO 0
+#define XGB_AOV_NORMAL 1
+xgb_status xgb_film_enable_aovs(xgb_film* film);
+xgb_status xgb_film_download_aov(xgb_film* film, int which, float* host, int pixel_stride_bytes, void* stream);
+
+/* ---------------------------------------------------------- image output */
+/* Display mapping of RTCamp8/Main.cpp:669-682 on the GPU: per channel
+ * clamp((int)(pow(v * exposure, 1 / gamma) * 255), 0, 255) with v = sum * scale
+ * (scale = 1 / spp; the reference uses exposure 0.3, gamma 2.2); NaN -> 0.
+ * rgb: host array of width * height * 3 bytes, film row 0 first. */
+xgb_status xgb_film_tonemap(xgb_film* film, float scale, float exposure, float gamma, unsigned char* rgb, void* stream);
+/* VisualizeError/Main.cpp:64-82 on two films of one size: t = (lum(a * scale_a)
+ * - lum(b * scale_b))^2 / max_value (rgbToLuminance weights, Vector.h:828-830),
+ * coloured by the Jet colormap; rgb as above. */
+xgb_status xgb_film_error_map(xgb_film* a, float scale_a, xgb_film* b, float scale_b, float max_value,
+                              unsigned char* rgb, void* stream);
+/* Writes an 8-bit RGB PNG (rows top to bottom), as stbi_write_png does for
+ * RTCamp8/Main.cpp:385-390; uncompressed deflate blocks. */
+xgb_status xgb_write_png(const char* path, int width, int height, const unsigned char* rgb);
 
 /* --------------------------------------------------------------- rendering */
 typedef enum { XGB_INTEGRATOR_STANDARD = 0, XGB_INTEGRATOR_NAIVE = 1 } xgb_integrator;

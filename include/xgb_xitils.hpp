@@ -244,9 +244,27 @@ public:
     }
     const int width, height;
 
-private:
+protected:
+    xgb_film* handle() const { return h_; }
     xgb_ctx* ctx_;
+
+private:
     xgb_film* h_ = nullptr;
+};
+
+// DenoisableRenderTarget (RenderTarget.h:131-145): radiance plus the first-hit
+// albedo and normal sums that a denoiser takes as auxiliary images.
+class DenoisableRenderTarget : public RenderTarget {
+public:
+    DenoisableRenderTarget(Context& ctx, int width, int height, bool fp64 = false) : RenderTarget(ctx, width, height, fp64) {
+        check(xgb_film_enable_aovs(handle()), ctx_, "DenoisableRenderTarget");
+    }
+    void downloadAlbedo(float* host, int strideBytes = 16, void* stream = nullptr) {
+        check(xgb_film_download_aov(handle(), XGB_AOV_ALBEDO, host, strideBytes, stream), ctx_, "downloadAlbedo");
+    }
+    void downloadNormal(float* host, int strideBytes = 16, void* stream = nullptr) {
+        check(xgb_film_download_aov(handle(), XGB_AOV_NORMAL, host, strideBytes, stream), ctx_, "downloadNormal");
+    }
 };
 
 }  // namespace xgb

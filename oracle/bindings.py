@@ -126,6 +126,24 @@ class CpuChecker:
             raise RuntimeError(f"{self.kind} render_pcg failed ({r})")
         return film
 
+    def render_pcg_aov(self, desc, spp_begin=0, spp_count=None, rect=None, nthreads=0, params=None):
+        """render_pcg plus the first-hit albedo and normal sums (DenoisableRenderTargetPixel).
+        Returns (film [H, W, 3], albedo [H, W, 3], normal [H, W, 3])."""
+        P = params or desc.params
+        W, H = desc.width, desc.height
+        x0, y0, x1, y1 = rect or (0, 0, W, H)
+        film = np.zeros((H, W, 3), dtype=np.float32)
+        aov = np.zeros((H, W, 6), dtype=np.float32)
+        n = desc.spp if spp_count is None else spp_count
+        r = self._call("render_pcg_aov", C.c_int(W), C.c_int(H), C.c_uint32(spp_begin), C.c_uint32(n),
+                       C.c_uint32(P.seed), C.c_int(P.integrator), C.c_int(P.max_depth), C.c_int(P.rr_start),
+                       C.c_float(P.rr_prob), C.c_int(x0), C.c_int(y0), C.c_int(x1), C.c_int(y1),
+                       film.ctypes.data_as(C.POINTER(C.c_float)), aov.ctypes.data_as(C.POINTER(C.c_float)),
+                       C.c_int(nthreads))
+        if r != 0:
+            raise RuntimeError(f"{self.kind} render_pcg_aov failed ({r})")
+        return film, aov[..., :3].copy(), aov[..., 3:].copy()
+
     def render_stock(self, W, H, spp, integrator=0, nthreads=0):
         """The reference's own RenderTarget::render (per-tile MT samplers). Returns (film, seconds)."""
         assert self.kind == "reference"

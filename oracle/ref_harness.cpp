@@ -266,9 +266,9 @@ int xref_build(void* p) {
 // Per-(pixel, sample) PCG render. Only the reference's defaults are available
 // (its Russian-roulette constants are private, PathTracer.h:253-257, and it has
 // no depth limit), so other parameter values are rejected.
-int xref_render_pcg(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
-                    int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
-                    int nthreads) {
+static int renderPcg(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                     int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                     float* aov, int nthreads) {
     RefScene* s = (RefScene*)p;
     if (!s->built || !s->scene.camera) return -1;
     if (max_depth != 0 || rr_start != 5 || rr_prob != 0.9f) return -2;
@@ -290,18 +290,45 @@ int xref_render_pcg(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_coun
             tile.offset = Vector2i((x / RenderTargetTile<Vector3f>::Width) * RenderTargetTile<Vector3f>::Width,
                                    (y / RenderTargetTile<Vector3f>::Height) * RenderTargetTile<Vector3f>::Height);
             Vector2i local(x - tile.offset.x, y - tile.offset.y);
-            Vector3f sum;
+            DenoisableRenderTargetPixel px;  // sum accumulation as in SimplePathTracerWithDenoiser/Main.cpp:144-151
             for (uint32_t k = 0; k < spp_count; ++k) {
                 sampler.seedPath(pixel, spp_begin + k, seed);
                 Vector2f pFilm = tile.GenerateFilmPosition(local, true);
                 Ray ray = s->scene.camera->generateRay(pFilm, sampler);
-                sum += pt.eval(s->scene, sampler, ray).color;
+                PathTracerEvalResult res = pt.eval(s->scene, sampler, ray);
+                px.color += res.color;
+                px.albedo += res.albedo;
+                px.normal += res.normal;
             }
-            float* px = film + 3 * (size_t)pixel;
-            px[0] += sum.x; px[1] += sum.y; px[2] += sum.z;
+            float* f = film + 3 * (size_t)pixel;
+            f[0] += px.color.x; f[1] += px.color.y; f[2] += px.color.z;
+            if (aov) {
+                float* q = aov + 6 * (size_t)pixel;
+                q[0] += px.albedo.x; q[1] += px.albedo.y; q[2] += px.albedo.z;
+                q[3] += px.normal.x; q[4] += px.normal.y; q[5] += px.normal.z;
+            }
         }
     }
     return 0;
+}
+
+// Per-(pixel, sample) PCG render. Only the reference's defaults are available
+// (its Russian-roulette constants are private, PathTracer.h:253-257, and it has
+// no depth limit), so other parameter values are rejected.
+int xref_render_pcg(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                    int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                    int nthreads) {
+    return renderPcg(p, W, H, spp_begin, spp_count, seed, integrator, max_depth, rr_start, rr_prob, x0, y0, x1, y1,
+                     film, nullptr, nthreads);
+}
+
+// The same render with DenoisableRenderTargetPixel's albedo and normal sums
+// (RenderTarget.h:131-145): aov is float[H][W][6].
+int xref_render_pcg_aov(void* p, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                        int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                        float* aov, int nthreads) {
+    return renderPcg(p, W, H, spp_begin, spp_count, seed, integrator, max_depth, rr_start, rr_prob, x0, y0, x1, y1,
+                     film, aov, nthreads);
 }
 
 // The reference's stock render call exactly as the sandboxes drive it

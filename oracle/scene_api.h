@@ -49,6 +49,10 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
     int P##build(void* s);                                                                         \
     int P##render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count,               \
                       uint32_t seed, int integrator, int max_depth, int rr_start, float rr_prob,   \
-                      int x0, int y0, int x1, int y1, float* film, int nthreads);
+                      int x0, int y0, int x1, int y1, float* film, int nthreads);              \
+    int P##render_pcg_aov(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count,           \
+                          uint32_t seed, int integrator, int max_depth, int rr_start,              \
+                          float rr_prob, int x0, int y0, int x1, int y1, float* film, float* aov,  \
+                          int nthreads);
 
 #endif

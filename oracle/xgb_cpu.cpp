@@ -938,11 +938,26 @@ struct Params {
 const float kRayOffset = 0.00001f;     // PathTracer.h:254
 const float kShadowMargin = 0.0001f;   // PathTracer.h:257
 
+// Material::getAlbedo (Material.h:44-47, 83-85, 129-131, 168-170, 380-382):
+// Diffuse albedo (times its texture), Glossy albedo, GlossyWithHighLight its
+// base's albedo, Metal f0; every other material (the sandbox's GlossyClamped
+// and MicrofacetNormalMapping included) keeps the zero default.
+V3 albedoOf(const Scene& sc, const Material& m, const Isect& is) {
+    switch (m.type) {
+    case ORC_MAT_DIFFUSE: return m.tex < 0 ? m.albedo : m.albedo * sc.textures[m.tex].lookup(is.uv);
+    case ORC_MAT_GLOSSY:
+    case ORC_MAT_GLOSSY_HIGHLIGHT: return m.albedo;
+    case ORC_MAT_METAL: return m.f0;
+    default: return V3(0.0f);
+    }
+}
+
 // StandardPathTracer::eval (PathTracer.h:117-251) with two additions that the
 // reference hard-codes: rrStart / rrProb (its russianRouletteLengthMin = 5,
 // russianRouletteProb = 0.9) and maxDepth (0 = unlimited, as in the reference:
 // the loop stops before vertex pathLength when pathLength > maxDepth).
-V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray) {
+// aov (optional): albedo and normal of the first hit (PathTracer.h:138-139).
+V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = nullptr) {
     Shading sh{&sc};
     V3 radiance(0.0f), weight(1.0f);
     Isect isect, next;
@@ -954,6 +969,10 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray) {
     }
     ++pathLength;
     const Material* mat = &sc.materials[sc.objects[isect.object].material];
+    if (aov) {
+        aov[0] = albedoOf(sc, *mat, isect);
+        aov[1] = isect.n;
+    }
     if (mat->emissive()) radiance = radiance + weight * emission(*mat, -ray.d, isect.n);
     while (true) {
         // An emitter's evalAndSample returns zero (Material.h:400-402): the
@@ -1029,7 +1048,8 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray) {
 }
 
 // NaivePathTracer::eval (PathTracer.h:50-104), same parameter additions.
-V3 evalNaive(const Scene& sc, const Params& P, Rng& rng, Ray ray) {
+// aov (optional): albedo and normal of the first hit (PathTracer.h:76-80).
+V3 evalNaive(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = nullptr) {
     Shading sh{&sc};
     V3 radiance(0.0f), weight(1.0f);
     Isect isect;
@@ -1043,6 +1063,10 @@ V3 evalNaive(const Scene& sc, const Params& P, Rng& rng, Ray ray) {
         }
         if (sceneIntersect(sc, ray, &isect)) {
             const Material& m = sc.materials[sc.objects[isect.object].material];
+            if (aov && pathLength == 1) {
+                aov[0] = albedoOf(sc, m, isect);
+                aov[1] = isect.n;
+            }
             if (m.emissive()) radiance = radiance + weight * emission(m, -ray.d, isect.n);
             float pdf;
             weight = weight * sh.evalAndSample(sc.objects[isect.object].material, isect, rng, &wi, &pdf);
@@ -1187,9 +1211,9 @@ int xcpu_build(void* s) {
 
 // Per-(pixel, sample) PCG render over the pixel rectangle [x0,x1) x [y0,y1).
 // Film position follows RenderTargetTile::GenerateFilmPosition (RenderTarget.h:68-80).
-int xcpu_render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
-                    int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
-                    int nthreads) {
+static int renderPcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                     int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                     float* aovFilm, int nthreads) {
     Scene* sc = (Scene*)s;
     if (!sc->built) return -1;
     Params P{integrator, max_depth, rr_start, rr_prob};
@@ -1201,7 +1225,7 @@ int xcpu_render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_coun
         Rng rng;
         for (int x = x0; x < x1; ++x) {
             uint32_t pixel = (uint32_t)(x + y * W);
-            V3 sum(0.0f);
+            V3 sum(0.0f), albedo(0.0f), normal(0.0f);
             for (uint32_t k = 0; k < spp_count; ++k) {
                 rng.seed(pixel, spp_begin + k, seed);
                 float fx = (float)x, fy = (float)y;
@@ -1211,14 +1235,41 @@ int xcpu_render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_coun
                 fx += (rng.randf() - 0.5f) / W;
                 fy += (rng.randf() - 0.5f) / H;
                 Ray r = cameraRay(*sc, fx, fy);
-                V3 c = integrator == ORC_INTEGRATOR_NAIVE ? evalNaive(*sc, P, rng, r) : evalStandard(*sc, P, rng, r);
+                V3 aov[2] = {V3(0.0f), V3(0.0f)};
+                V3* a = aovFilm ? aov : nullptr;
+                V3 c = integrator == ORC_INTEGRATOR_NAIVE ? evalNaive(*sc, P, rng, r, a) : evalStandard(*sc, P, rng, r, a);
                 sum = sum + c;
+                albedo = albedo + aov[0];
+                normal = normal + aov[1];
             }
             float* px = film + 3 * (size_t)pixel;
             px[0] += sum.x; px[1] += sum.y; px[2] += sum.z;
+            if (aovFilm) {
+                float* q = aovFilm + 6 * (size_t)pixel;
+                q[0] += albedo.x; q[1] += albedo.y; q[2] += albedo.z;
+                q[3] += normal.x; q[4] += normal.y; q[5] += normal.z;
+            }
         }
     }
     return 0;
+}
+
+// Per-(pixel, sample) PCG render over the pixel rectangle [x0,x1) x [y0,y1).
+// Film position follows RenderTargetTile::GenerateFilmPosition (RenderTarget.h:68-80).
+int xcpu_render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                    int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                    int nthreads) {
+    return renderPcg(s, W, H, spp_begin, spp_count, seed, integrator, max_depth, rr_start, rr_prob, x0, y0, x1, y1,
+                     film, nullptr, nthreads);
+}
+
+// The same render accumulating DenoisableRenderTargetPixel's albedo and normal
+// (RenderTarget.h:131-145) as well: aov is float[H][W][6] (albedo rgb, normal xyz).
+int xcpu_render_pcg_aov(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count, uint32_t seed, int integrator,
+                        int max_depth, int rr_start, float rr_prob, int x0, int y0, int x1, int y1, float* film,
+                        float* aov, int nthreads) {
+    return renderPcg(s, W, H, spp_begin, spp_count, seed, integrator, max_depth, rr_start, rr_prob, x0, y0, x1, y1,
+                     film, aov, nthreads);
 }
 
 // Closest-hit query for traversal known-answer tests: rays are float[n][7]

@@ -1,5 +1,6 @@
 // Renders a small scene through include/xgb_xitils.hpp (the C++ adapter with
-// Xitils' class names) and writes the film sums to argv[1] as float32 RGB.
+// Xitils' class names) into a DenoisableRenderTarget and writes the film sums
+// to argv[1] as float32 RGB, then the first-hit albedo and normal sums after them.
 // The scene matches tests/test_cpp_adapter.py::scene_desc(): a light quad facing
 // -y above a Diffuse floor quad and a unit cube (the reference's Cube indices)
 // scaled 0.4 and rotated, camera looking along +z.
@@ -52,13 +53,17 @@ int main(int argc, char** argv) {
         const float sky[3] = {0.1f, 0.12f, 0.15f};
         scene.setSkyUniform(sky);
         scene.buildAccelerationStructure();
-        xgb::RenderTarget film(gpu, W, H);
+        xgb::DenoisableRenderTarget film(gpu, W, H);
         xgb::StandardPathTracer tracer;
         film.render(scene, SPP / 2, tracer, 0);
         film.render(scene, SPP / 2, tracer, SPP / 2);  // progressive: two sample ranges add up
         std::vector<float> host(4 * W * H);
         film.download(host.data(), 16);  // xitils::Vector3f layout
         FILE* f = std::fopen(argv[1], "wb");
+        for (int i = 0; i < W * H; ++i) std::fwrite(&host[4 * i], 4, 3, f);
+        film.downloadAlbedo(host.data(), 16);
+        for (int i = 0; i < W * H; ++i) std::fwrite(&host[4 * i], 4, 3, f);
+        film.downloadNormal(host.data(), 16);
         for (int i = 0; i < W * H; ++i) std::fwrite(&host[4 * i], 4, 3, f);
         std::fclose(f);
         std::printf("ok %d %d %d\n", W, H, SPP);

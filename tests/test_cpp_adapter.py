@@ -61,7 +61,10 @@ def test_adapter_renders_like_oracle(tmp_path):
     r = subprocess.run([exe, out], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     desc = scene_desc()
-    film = np.fromfile(out, dtype=np.float32).reshape(desc.height, desc.width, 3)
-    ref = load_scene(desc, "port").render_pcg(desc)
+    planes = np.fromfile(out, dtype=np.float32).reshape(3, desc.height, desc.width, 3)
+    film, albedo, normal = planes
+    ref, ref_albedo, ref_normal = load_scene(desc, "port").render_pcg_aov(desc)
     assert np.isfinite(film).all()
     assert relmse(film, ref) <= 1e-4
+    np.testing.assert_allclose(albedo, ref_albedo, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(normal, ref_normal, rtol=1e-5, atol=1e-5)

@@ -122,3 +122,31 @@ def test_small_queue_capacity_same_image(ctx):
     np.testing.assert_allclose(small.download(), big.download(), rtol=1e-4, atol=1e-5)
     st = b.scene.stats()
     assert st["paths"] == 40 * 40 * 4 and st["error_flags"] == 0
+
+
+@pytest.mark.parametrize("make,params,color_tol", [
+    (lambda: scenes.cornell(64, 64, 4), IntegratorParams(), TOL),
+    (lambda: scenes.cornell(48, 48, 4), IntegratorParams(integrator=NAIVE), TOL),
+    # every material kind, microfacet normal mapping included (its radiance gate)
+    (lambda: scenes.material_zoo(64, 64, 4, sky="latlong"), IntegratorParams(), MFNM_TOL),
+    (lambda: scenes.terrain(grid=65, width=48, height=48, spp=4, env_size=(128, 64)), IntegratorParams(), TOL),
+])
+def test_denoiser_aovs(ctx, make, params, color_tol):
+    """First-hit albedo and normal sums (DenoisableRenderTarget) against the
+    oracle: the first hit is the same triangle with the same barycentrics, so
+    only the order of the per-pixel sums differs (FP32 atomics)."""
+    from xitils_gb300 import api
+    desc = make()
+    rt = api.RenderTarget(ctx, desc.width, desc.height, aovs=True)
+    b = api.load_scene(ctx, desc)
+    rt.render(b.scene, desc.spp, params, 0)
+    color, albedo, normal = rt.download(), rt.download_aov("albedo"), rt.download_aov("normal")
+    c_cpu, a_cpu, n_cpu = load_cpu(desc, "port").render_pcg_aov(desc, params=params)
+    np.testing.assert_allclose(albedo, a_cpu, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(normal, n_cpu, rtol=1e-5, atol=1e-5)
+    assert relmse(color, c_cpu) <= color_tol
+    plain = api.render_desc(ctx, desc, params=params, builder=b)
+    np.testing.assert_array_equal(np.isfinite(plain), True)
+    assert relmse(plain, color) <= 1e-9  # enabling the AOV planes leaves the radiance alone
+    rt.clear()
+    assert not rt.download_aov("albedo").any() and not rt.download_aov("normal").any()

@@ -184,3 +184,76 @@ def test_training_concentrates_on_the_target(guide):
                                      np.ones(n, np.float32), lr=3e-3))
     assert np.isfinite(losses).all()
     assert np.mean(losses[-20:]) < losses[0] - 1.5, (losses[0], np.mean(losses[-20:]))
+
+
+def _fixture_mixture():
+    import os
+    f = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_aov_vmf.npz"))
+    enc = f["vmf_encoded"].astype(np.float64)
+    mu = np.stack([enc[5 * j:5 * j + 3] for j in range(8)])
+    kappa = np.array([enc[5 * j + 3] for j in range(8)])
+    alpha = np.array([enc[5 * j + 4] for j in range(7)] + [0.0])
+    alpha[7] = 1.0 - alpha[:7].sum()
+    return f, mu, kappa, alpha
+
+
+def _mixture_pdf(mu, kappa, alpha, w):
+    w = np.asarray(w, np.float64).reshape(-1, 1, 3)
+    k = np.where(kappa > 0, kappa, 1.0)
+    v = np.where(kappa > 0, G.vmf_pdf(mu, k, w), 1.0 / (4 * np.pi))
+    return np.sum(alpha * v, axis=1)
+
+
+def test_numpy_vmf_matches_reference_fit_fixture():
+    """The FP64 restatement of the mixture pdf against the reference's own
+    VonMisesFisherDistribution<8>::eval on its EM fit (tests/golden)."""
+    f, mu, kappa, alpha = _fixture_mixture()
+    assert np.all(kappa >= 0) and np.isclose(alpha.sum(), 1.0)
+    np.testing.assert_allclose(_mixture_pdf(mu, kappa, alpha, f["vmf_dirs"]), f["vmf_pdf"], rtol=2e-5, atol=1e-7)
+    # the fit describes its own samples better than a uniform hemisphere does
+    assert np.mean(np.log(f["vmf_sample_pdf"])) > np.log(1 / (2 * np.pi))
+
+
+@pytest.mark.gpu
+def test_gpu_mixture_of_reference_fit(guide):
+    """A network whose output layer is the reference's EM fit (zero weights,
+    biases = the fit): the GPU decodes that mixture, its pdf matches the
+    reference's eval, and its samples follow it."""
+    from xitils_gb300 import api
+    ctx, _ = guide
+    f, mu, kappa, alpha = _fixture_mixture()
+    assert np.all((kappa > np.exp(G.KMIN)) & (kappa < np.exp(G.KMAX)))
+    gd = api.Guide(ctx, seed=2)
+    gd.set_bounds(LO, HI)
+    d = G.split(gd.params().astype(np.float64))
+    d["W3"][:] = 0.0
+    b3 = d["b3"].reshape(8, 5)
+    b3[:, 0:3] = mu
+    b3[:, 3] = np.log(kappa)
+    b3[:, 4] = np.log(alpha)
+    gd.set_params(G.join(d).astype(np.float32))
+    n = 60000
+    pos = np.tile(np.array([[0.1, 0.2, 0.3]], np.float32), (n, 1))
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (n, 1))
+    wo = nrm.copy()
+    Y = gd.infer(pos[:1], nrm[:1], wo[:1])
+    gmu, gk, ga = G.decode(Y)
+    np.testing.assert_allclose(gmu[0], mu / np.linalg.norm(mu, axis=1, keepdims=True), atol=1e-6)
+    np.testing.assert_allclose(gk[0], kappa, rtol=1e-5)
+    np.testing.assert_allclose(ga[0], alpha, rtol=1e-5, atol=1e-7)
+    dirs, pdf = gd.sample(pos[:n // 2], nrm[:n // 2], wo[:n // 2], seed=5)
+    dirs2, pdf2 = gd.sample(pos[n // 2:], nrm[n // 2:], wo[n // 2:], seed=6)
+    dirs = np.concatenate([dirs, dirs2]).astype(np.float64)
+    pdf = np.concatenate([pdf, pdf2])
+    np.testing.assert_allclose(pdf, _mixture_pdf(mu, kappa, alpha, dirs), rtol=2e-3, atol=1e-6)
+    # octant histogram against the reference's pdf integrated over each octant
+    rng = np.random.default_rng(0)
+    u = rng.normal(size=(400000, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    p = _mixture_pdf(mu, kappa, alpha, u)
+    octant = lambda v: (v[:, 0] > 0).astype(int) * 4 + (v[:, 1] > 0) * 2 + (v[:, 2] > 0)
+    expected = np.bincount(octant(u), weights=p * 4 * np.pi / u.shape[0], minlength=8) * n
+    observed = np.bincount(octant(dirs), minlength=8)
+    mask = expected > 50
+    chi2 = np.sum((observed[mask] - expected[mask]) ** 2 / expected[mask])
+    assert chi2 < 40, (observed, expected)

@@ -108,3 +108,28 @@ def test_mfnm_amplifies_last_ulp_differences():
     a = load_scene(cb, "port").render_pcg(cb)
     b = load_scene(cb, "port_ulp").render_pcg(cb)
     assert relmse(b, a) < 1e-4
+
+
+GOLDEN_AOV = os.path.join(os.path.dirname(__file__), "golden", "reference_aov_vmf.npz")
+AOV_CASES = {
+    "cornell_40x40x3": (lambda: scenes.cornell(40, 40, 3), IntegratorParams()),
+    "cornell_naive_32x32x3": (lambda: scenes.cornell(32, 32, 3), IntegratorParams(integrator=NAIVE)),
+    "zoo_latlong_40x40x2": (lambda: scenes.material_zoo(40, 40, 2, sky="latlong"), IntegratorParams()),
+    "terrain_g65_32x32x2": (lambda: scenes.terrain(grid=65, width=32, height=32, spp=2, env_size=(128, 64)),
+                            IntegratorParams()),
+}
+
+
+@pytest.mark.parametrize("name", sorted(AOV_CASES))
+def test_oracle_aovs_match_golden(name):
+    """DenoisableRenderTargetPixel sums (color, first-hit albedo, normal) of the
+    reference, bit for bit."""
+    golden = np.load(GOLDEN_AOV)
+    make, params = AOV_CASES[name]
+    desc = make()
+    film, albedo, normal = load_scene(desc, "port").render_pcg_aov(desc, params=params)
+    assert np.array_equal(film, golden[name + "_color"])
+    assert np.array_equal(albedo, golden[name + "_albedo"])
+    assert np.array_equal(normal, golden[name + "_normal"])
+    plain = load_scene(desc, "port").render_pcg(desc, params=params)
+    assert np.array_equal(plain, film)  # the AOVs draw nothing from the paths' streams

@@ -62,6 +62,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_ctx_create": [C.c_int, C.POINTER(P)],
         "xgb_ctx_destroy": [P],
         "xgb_ctx_synchronize": [P, P],
+        "xgb_film_enable_aovs": [P],
+        "xgb_film_tonemap": [P, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_uint8), P],
+        "xgb_film_error_map": [P, C.c_float, P, C.c_float, C.c_float, C.POINTER(C.c_uint8), P],
+        "xgb_write_png": [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_uint8)],
+        "xgb_film_download_aov": [P, C.c_int, FP, C.c_int, P],
         "xgb_texture_create": [P, C.c_int, C.c_int, C.c_int, FP, C.c_int, C.c_int, C.POINTER(P)],
         "xgb_texture_destroy": [P],
         "xgb_mesh_create": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(P)],
@@ -342,12 +347,41 @@ class Scene:
 
 
 class RenderTarget:
-    """Per-pixel radiance sums on the GPU (RenderTarget<Vector3f>)."""
+    """Per-pixel radiance sums on the GPU (RenderTarget<Vector3f>); with
+    ``aovs=True`` also the first-hit albedo and normal sums of a
+    DenoisableRenderTarget (RenderTarget.h:131-145)."""
 
-    def __init__(self, ctx: Context, width: int, height: int, fp64: bool = False):
+    AOV = {"albedo": 0, "normal": 1}
+
+    def __init__(self, ctx: Context, width: int, height: int, fp64: bool = False, aovs: bool = False):
         self.ctx, self.width, self.height = ctx, width, height
         self.h = P()
         ctx.check(ctx.lib.xgb_film_create(ctx.h, width, height, int(fp64), C.byref(self.h)), "RenderTarget")
+        if aovs:
+            ctx.check(ctx.lib.xgb_film_enable_aovs(self.h), "enable_aovs")
+
+    def tonemap(self, scale: float = 1.0, exposure: float = 0.3, gamma: float = 2.2, stream=None) -> np.ndarray:
+        """8-bit display image [H, W, 3] (RTCamp8's mapping; scale = 1 / spp)."""
+        out = np.empty((self.height, self.width, 3), np.uint8)
+        self.ctx.check(self.ctx.lib.xgb_film_tonemap(self.h, C.c_float(scale), C.c_float(exposure), C.c_float(gamma),
+                                                     out.ctypes.data_as(C.POINTER(C.c_uint8)), stream), "tonemap")
+        return out
+
+    def error_map(self, other: "RenderTarget", scale: float, other_scale: float, max_value: float,
+                  stream=None) -> np.ndarray:
+        """Jet-coloured squared luminance difference against another film [H, W, 3] uint8."""
+        out = np.empty((self.height, self.width, 3), np.uint8)
+        self.ctx.check(self.ctx.lib.xgb_film_error_map(self.h, C.c_float(scale), other.h, C.c_float(other_scale),
+                                                       C.c_float(max_value), out.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                       stream), "error_map")
+        return out
+
+    def download_aov(self, which: str, out: Optional[np.ndarray] = None, stream=None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == self.width * self.height * 3
+        self.ctx.check(self.ctx.lib.xgb_film_download_aov(self.h, self.AOV[which], _fp(out), 12, stream), "download_aov")
+        return out
 
     def clear(self, stream=None):
         self.ctx.check(self.ctx.lib.xgb_film_clear(self.h, stream), "clear")
@@ -370,6 +404,16 @@ class RenderTarget:
         f = C.c_int()
         self.ctx.check(self.ctx.lib.xgb_film_device_pointer(self.h, C.byref(p), C.byref(f)), "device_pointer")
         return p.value, bool(f.value)
+
+
+def write_png(path: str, rgb: np.ndarray) -> None:
+    """8-bit RGB PNG (xgb_write_png)."""
+    lib = load_library()
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w = rgb.shape[:2]
+    st = lib.xgb_write_png(path.encode(), w, h, rgb.ctypes.data_as(C.POINTER(C.c_uint8)))
+    if st != 0:
+        raise XgbError(st, f"write_png({path}) failed")
 
 
 class Guide:

@@ -130,6 +130,7 @@ struct xgb_film {
     xgb_ctx* ctx;
     int w = 0, h = 0, fp64 = 0;
     void* d = nullptr;
+    void* aov = nullptr;  // albedo plane then normal plane, same element type as d
 };
 
 struct xgb_guide {
@@ -836,33 +837,60 @@ xgb_status xgb_film_create(xgb_ctx* ctx, int width, int height, int fp64, xgb_fi
 xgb_status xgb_film_destroy(xgb_film* f) {
     if (!f) return XGB_INVALID_ARG;
     dfree(f->d);
+    dfree(f->aov);
     delete f;
     return XGB_OK;
 }
+static size_t filmPlaneBytes(const xgb_film* f) { return (size_t)f->w * f->h * (f->fp64 ? 32 : 16); }
 xgb_status xgb_film_clear(xgb_film* f, void* stream) {
     if (!f) return XGB_INVALID_ARG;
-    XGB_CUDA(f->ctx, cudaMemsetAsync(f->d, 0, (size_t)f->w * f->h * (f->fp64 ? 32 : 16), pick(f->ctx, stream)));
+    XGB_CUDA(f->ctx, cudaMemsetAsync(f->d, 0, filmPlaneBytes(f), pick(f->ctx, stream)));
+    if (f->aov) XGB_CUDA(f->ctx, cudaMemsetAsync(f->aov, 0, 2 * filmPlaneBytes(f), pick(f->ctx, stream)));
     return XGB_OK;
 }
-xgb_status xgb_film_download(xgb_film* f, float* host, int stride, void* stream) {
-    if (!f || !host || (stride != 12 && stride != 16)) return fail(f ? f->ctx : nullptr, XGB_INVALID_ARG, "xgb_film_download: bad arguments");
-    cudaStream_t st = pick(f->ctx, stream);
+static xgb_status downloadPlane(xgb_film* f, const void* src, float* host, int stride, cudaStream_t st) {
     size_t n = (size_t)f->w * f->h;
     const int fs = stride / 4;
     if (f->fp64) {
         std::vector<double> tmp(4 * n);
-        XGB_CUDA(f->ctx, cudaMemcpyAsync(tmp.data(), f->d, 32 * n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaMemcpyAsync(tmp.data(), src, 32 * n, cudaMemcpyDeviceToHost, st));
         XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
         for (size_t i = 0; i < n; ++i)
             for (int k = 0; k < 3; ++k) host[fs * i + k] = (float)tmp[4 * i + k];
     } else if (stride == 16) {
-        XGB_CUDA(f->ctx, cudaMemcpyAsync(host, f->d, 16 * n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaMemcpyAsync(host, src, 16 * n, cudaMemcpyDeviceToHost, st));
         XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
     } else {
-        XGB_CUDA(f->ctx, cudaMemcpy2DAsync(host, 12, f->d, 16, 12, n, cudaMemcpyDeviceToHost, st));
+        XGB_CUDA(f->ctx, cudaMemcpy2DAsync(host, 12, src, 16, 12, n, cudaMemcpyDeviceToHost, st));
         XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
     }
     return XGB_OK;
+}
+xgb_status xgb_film_download(xgb_film* f, float* host, int stride, void* stream) {
+    if (!f || !host || (stride != 12 && stride != 16)) return fail(f ? f->ctx : nullptr, XGB_INVALID_ARG, "xgb_film_download: bad arguments");
+    return downloadPlane(f, f->d, host, stride, pick(f->ctx, stream));
+}
+xgb_status xgb_film_enable_aovs(xgb_film* f) {
+    if (!f) return XGB_INVALID_ARG;
+    if (f->aov) return XGB_OK;
+    cudaSetDevice(f->ctx->device);
+    cudaError_t e = cudaMalloc(&f->aov, 2 * filmPlaneBytes(f));
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->aov, 0, 2 * filmPlaneBytes(f), f->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(f->ctx->stream);
+    if (e != cudaSuccess) {
+        dfree(f->aov);
+        f->aov = nullptr;
+        return e == cudaErrorMemoryAllocation ? fail(f->ctx, XGB_OOM, "xgb_film_enable_aovs: out of memory")
+                                              : cudaFail(f->ctx, e, "xgb_film_enable_aovs");
+    }
+    return XGB_OK;
+}
+xgb_status xgb_film_download_aov(xgb_film* f, int which, float* host, int stride, void* stream) {
+    if (!f || !host || (stride != 12 && stride != 16) || (which != XGB_AOV_ALBEDO && which != XGB_AOV_NORMAL))
+        return fail(f ? f->ctx : nullptr, XGB_INVALID_ARG, "xgb_film_download_aov: bad arguments");
+    if (!f->aov) return fail(f->ctx, XGB_INVALID_ARG, "xgb_film_download_aov: call xgb_film_enable_aovs first");
+    const char* base = (const char*)f->aov + (which == XGB_AOV_NORMAL ? filmPlaneBytes(f) : 0);
+    return downloadPlane(f, base, host, stride, pick(f->ctx, stream));
 }
 xgb_status xgb_film_device_pointer(xgb_film* f, void** out, int* is_fp64) {
     if (!f || !out) return XGB_INVALID_ARG;
@@ -953,6 +981,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.capacity = cap;
     rp.filmFp64 = film->fp64;
     rp.film = film->d;
+    rp.aov = film->aov;
     rp.guided = 0;
     rp.train = 0;
     rp.bsdfFrac = s->bsdfFrac;
@@ -1127,6 +1156,16 @@ bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp
     *w = f->w;
     *h = f->h;
     *fp64 = f->fp64;
+    return true;
+}
+bool filmPlane(xgb_film* f, void** d, int* w, int* h, int* fp64, int* device, cudaStream_t* ctxStream) {
+    if (!f) return false;
+    *d = f->d;
+    *w = f->w;
+    *h = f->h;
+    *fp64 = f->fp64;
+    *device = f->ctx->device;
+    *ctxStream = f->ctx->stream;
     return true;
 }
 }  // namespace xgb

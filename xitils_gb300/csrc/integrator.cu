@@ -32,6 +32,20 @@ __device__ __forceinline__ void filmAddS(const RenderParams& rp, int pix, V3 c) 
     }
 }
 
+// DenoisableRenderTarget planes: first-hit albedo, then first-hit normal.
+__device__ __forceinline__ void aovAdd(const RenderParams& rp, int pix, V3 albedo, V3 normal) {
+    const size_t plane = (size_t)rp.width * (size_t)rp.height;
+    if (rp.filmFp64) {
+        double* a = (double*)rp.aov + 4 * (size_t)pix;
+        double* n = (double*)rp.aov + 4 * (plane + (size_t)pix);
+        atomicAdd(a, (double)albedo.x); atomicAdd(a + 1, (double)albedo.y); atomicAdd(a + 2, (double)albedo.z);
+        atomicAdd(n, (double)normal.x); atomicAdd(n + 1, (double)normal.y); atomicAdd(n + 2, (double)normal.z);
+    } else {
+        atomicAdd((float4*)rp.aov + pix, make_float4(albedo.x, albedo.y, albedo.z, 0.0f));
+        atomicAdd((float4*)rp.aov + plane + pix, make_float4(normal.x, normal.y, normal.z, 0.0f));
+    }
+}
+
 __global__ void k_plan(Ctrl* c, unsigned int capacity) {
     unsigned int nCont = c->nOut;
     unsigned long long remain = c->totalPaths - c->nextPath;
@@ -225,6 +239,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                 const Material& mat = sc.materials[inst.material];
                 Surface s = makeSurface(sc, inst, prim, h.y, h.z, dir);
                 const bool emissive = mat.kind == MAT_EMISSION;
+                if (rp.aov && (flags & FLAG_PRIMARY)) aovAdd(rp, pix, albedoOf(sc, mat, s), s.n);
                 if (naive) {
                     // NaivePathTracer::eval (PathTracer.h:75-100): emission, BSDF sample,
                     // then the next loop top (depth limit, Russian roulette) before tracing.

@@ -103,6 +103,7 @@ struct RenderParams {
     unsigned int capacity;
     int filmFp64;
     void* film;  // float4* or double4*
+    void* aov;   // first-hit albedo plane then normal plane (same type as film), nullptr: off
     // learned proposal (0 / nullptr when off)
     int guided;
     int train;
