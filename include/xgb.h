@@ -43,6 +43,13 @@ typedef struct xgb_film xgb_film;
 /* One context per GPU (and per host thread, or serialise calls on it). */
 xgb_status xgb_ctx_create(int device, xgb_ctx** out);
 xgb_status xgb_ctx_destroy(xgb_ctx* ctx);
+/* Builder of the per-mesh BVH for meshes created afterwards (the tree shape
+ * changes speed only, never the image): XGB_BVH_PLOC (default, locally-ordered
+ * clustering by surface area) or XGB_BVH_LBVH (Morton-code splits). The
+ * reference builds a single-threaded top-down tree (AccelerationStructure.h:163-291). */
+#define XGB_BVH_PLOC 0
+#define XGB_BVH_LBVH 1
+xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder);
 /* Waits for the work enqueued on stream (NULL = the context's own stream). */
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream);
 /* Last error message of this context ("" when none). Never NULL. */
@@ -273,6 +280,15 @@ xgb_status xgb_guide_train_steps(xgb_guide* guide, uint64_t* out);
  * xgb_guide_set_training; standard integrator only; the call then holds 16
  * bytes of device memory per camera path). guide = NULL turns guiding off. */
 xgb_status xgb_scene_set_guide(xgb_scene* scene, xgb_guide* guide, float bsdf_fraction, int train, float learning_rate);
+
+/* Scene::intersect / Scene::intersectAny (Scene.h:30-38) for host arrays of n
+ * rays, float[n][7] = origin, direction, tMax. xgb_scene_intersect writes
+ * float[n][5] = (t of the closest hit, object index in xgb_scene_add_object
+ * order, triangle index within its mesh, barycentrics b0, b1); a miss gives
+ * (tMax, -1, -1, 0, 0). xgb_scene_occluded writes 1 where something is hit
+ * within tMax, else 0. Synchronises the stream. */
+xgb_status xgb_scene_intersect(xgb_scene* scene, int n, const float* rays, float* hits, void* stream);
+xgb_status xgb_scene_occluded(xgb_scene* scene, int n, const float* rays, int32_t* occluded, void* stream);
 
 /* enable = 1: later xgb_render calls on this scene record CUDA events around
  * every kernel on the render stream and count BVH work (for profiling; adds a

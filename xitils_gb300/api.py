@@ -62,6 +62,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_ctx_create": [C.c_int, C.POINTER(P)],
         "xgb_ctx_destroy": [P],
         "xgb_ctx_synchronize": [P, P],
+        "xgb_ctx_set_bvh_builder": [P, C.c_int],
+        "xgb_scene_intersect": [P, C.c_int, FP, FP, P],
+        "xgb_scene_occluded": [P, C.c_int, FP, C.POINTER(C.c_int32), P],
         "xgb_film_enable_aovs": [P],
         "xgb_film_tonemap": [P, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_uint8), P],
         "xgb_film_error_map": [P, C.c_float, P, C.c_float, C.c_float, C.POINTER(C.c_uint8), P],
@@ -156,6 +159,12 @@ class Context:
         if st != 0:
             msg = self.lib.xgb_get_last_error(self.h).decode()
             raise XgbError(st, f"{what}: {msg}")
+
+    BVH_BUILDERS = {"ploc": 0, "lbvh": 1}
+
+    def set_bvh_builder(self, name: str):
+        """BVH builder for meshes created afterwards: "ploc" (default) or "lbvh"."""
+        self.check(self.lib.xgb_ctx_set_bvh_builder(self.h, self.BVH_BUILDERS[name]), "set_bvh_builder")
 
     def synchronize(self, stream=None):
         self.check(self.lib.xgb_ctx_synchronize(self.h, stream), "synchronize")
@@ -332,6 +341,21 @@ class Scene:
         self.ctx.check(self.ctx.lib.xgb_scene_set_guide(self.h, guide.h if guide else None, C.c_float(bsdf_fraction),
                                                         int(train), C.c_float(lr)), "setGuide")
         self._guide = guide
+
+    def intersect(self, rays, stream=None) -> np.ndarray:
+        """Closest hits of float32 [n, 7] rays (o, d, tMax) -> [n, 5] (t, object, triangle, b0, b1)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 7)
+        hits = np.zeros((rays.shape[0], 5), np.float32)
+        self.ctx.check(self.ctx.lib.xgb_scene_intersect(self.h, rays.shape[0], _fp(rays), _fp(hits), stream),
+                       "intersect")
+        return hits
+
+    def occluded(self, rays, stream=None) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 7)
+        out = np.zeros(rays.shape[0], np.int32)
+        self.ctx.check(self.ctx.lib.xgb_scene_occluded(self.h, rays.shape[0], _fp(rays),
+                                                       out.ctypes.data_as(C.POINTER(C.c_int32)), stream), "occluded")
+        return out
 
     def set_profiling(self, enable: bool = True):
         self.ctx.check(self.ctx.lib.xgb_scene_set_profiling(self.h, int(enable)), "set_profiling")

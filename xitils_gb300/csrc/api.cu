@@ -92,6 +92,7 @@ struct xgb_ctx {
     int numSMs = 1;
     cudaStream_t stream = nullptr;
     std::string err;
+    int bvhBuilder = kBuilderPloc;
 };
 
 struct xgb_texture {
@@ -241,6 +242,14 @@ xgb_status xgb_ctx_destroy(xgb_ctx* ctx) {
     return XGB_OK;
 }
 
+xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder) {
+    if (!ctx) return XGB_INVALID_ARG;
+    if (builder != XGB_BVH_PLOC && builder != XGB_BVH_LBVH)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_bvh_builder: unknown builder");
+    ctx->bvhBuilder = builder == XGB_BVH_PLOC ? kBuilderPloc : kBuilderLbvh;
+    return XGB_OK;
+}
+
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream) {
     if (!ctx) return XGB_INVALID_ARG;
     XGB_CUDA(ctx, cudaStreamSynchronize(pick(ctx, stream)));
@@ -355,7 +364,7 @@ xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* position
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->dTris, sizeof(TriV) * m->nTris);
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->dNodes, sizeof(Node2) * std::max(1, m->nTris - 1));
     if (e == cudaSuccess) {
-        BlasBuildInput in{m->dPos, m->dIdx, m->nTris};
+        BlasBuildInput in{m->dPos, m->dIdx, m->nTris, ctx->bvhBuilder};
         BlasBuildOutput o{};
         o.nodes = m->dNodes; o.tris = m->dTris; o.gnrm = m->dGnrm; o.triArea = m->dArea;
         e = buildBlas(in, &o, s);
@@ -1121,6 +1130,62 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     if (c.errors & ERR_STACK) return fail(ctx, XGB_QUEUE_OVERFLOW, "xgb_render: traversal stack overflow");
     if (c.errors & ERR_LOOP) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: traversal iteration bound exceeded");
     return XGB_OK;
+}
+
+static xgb_status sceneQuery(xgb_scene* s, int n, const float* rays, int any, float* hits, int32_t* occ, void* stream) {
+    if (!s || n < 0 || !rays || (!any && !hits) || (any && !occ)) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = s->ctx;
+    if (!s->built) return fail(ctx, XGB_NOT_BUILT, "xgb_scene_intersect: call xgb_scene_build first");
+    if (n == 0) return XGB_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick(ctx, stream);
+    std::vector<float4> h(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays + 7 * (size_t)i;
+        h[i] = make_float4(r[0], r[1], r[2], r[6]);
+        h[(size_t)n + i] = make_float4(r[3], r[4], r[5], 0.0f);
+    }
+    char* dev = nullptr;
+    const size_t rayBytes = 32 * (size_t)n, outBytes = any ? 4 * (size_t)n : 32 * (size_t)n;
+    if (cudaMallocAsync((void**)&dev, rayBytes + outBytes + 256, st) != cudaSuccess)
+        return fail(ctx, XGB_OOM, "xgb_scene_intersect: out of device memory");
+    float4* dRays = (float4*)dev;
+    char* dOut = dev + rayBytes;
+    unsigned int* dErr = (unsigned int*)(dev + rayBytes + outBytes);
+    cudaError_t e = cudaMemcpyAsync(dRays, h.data(), rayBytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dErr, 0, 4, st);
+    unsigned int err = 0;
+    std::vector<float4> out(any ? 0 : 2 * (size_t)n);
+    if (e == cudaSuccess) {
+        launchQuery(s->sd, dRays, dRays + n, n, any, (float4*)dOut, (int*)dOut, dErr, ctx->numSMs * 8, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = any ? cudaMemcpyAsync(occ, dOut, 4 * (size_t)n, cudaMemcpyDeviceToHost, st)
+                                  : cudaMemcpyAsync(out.data(), dOut, 32 * (size_t)n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, dErr, 4, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(dev, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "xgb_scene_intersect");
+    if (!any)
+        for (int i = 0; i < n; ++i) {
+            const float4 a = out[2 * (size_t)i], b = out[2 * (size_t)i + 1];
+            float* o = hits + 5 * (size_t)i;
+            int inst, prim;
+            std::memcpy(&inst, &a.y, 4);
+            std::memcpy(&prim, &a.z, 4);
+            o[0] = a.x; o[1] = (float)inst; o[2] = (float)prim; o[3] = b.x; o[4] = b.y;
+        }
+    if (err & ERR_STACK) return fail(ctx, XGB_QUEUE_OVERFLOW, "xgb_scene_intersect: traversal stack overflow");
+    if (err & ERR_LOOP) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_scene_intersect: traversal iteration bound exceeded");
+    return XGB_OK;
+}
+
+xgb_status xgb_scene_intersect(xgb_scene* s, int n, const float* rays, float* hits, void* stream) {
+    return sceneQuery(s, n, rays, 0, hits, nullptr, stream);
+}
+
+xgb_status xgb_scene_occluded(xgb_scene* s, int n, const float* rays, int32_t* occluded, void* stream) {
+    return sceneQuery(s, n, rays, 1, nullptr, occluded, stream);
 }
 
 xgb_status xgb_scene_set_profiling(xgb_scene* s, int enable) {

@@ -2,16 +2,25 @@
 // builds its _BVH single-threaded on the CPU, AccelerationStructure.h:163-291;
 // the tree shape affects speed only, never the image).
 //
-// Linear BVH after Karras, "Maximizing Parallelism in the Construction of
-// BVHs, Octrees, and k-d Trees" (HPG 2012):
+// Two builders share steps 1-2 and the output format:
 //   1. per triangle: bounds, centroid, FP64-cross geometric normal, area;
 //   2. 30-bit Morton codes of the centroids, radix-sorted (CUB);
-//   3. one thread per internal node finds its key range and split;
-//   4. bounds propagate bottom-up (the second child to arrive merges);
-//   5. subtrees of <= kLeafMax triangles collapse into leaves and each inner
-//      node is written as a 64-byte Node2 holding both children's boxes;
-//   6. triangle vertices are gathered into leaf order (48 B per triangle).
+// PLOC (default), Meister & Bittner, "Parallel Locally-Ordered Clustering for
+// Bounding Volume Hierarchy Construction" (TVCG 2018): clusters start as the
+// sorted triangles; every round each cluster finds the neighbour within
+// kPlocRadius positions of the sorted order whose merged box has the smallest
+// surface area, mutual nearest neighbours merge into a new node, and the
+// cluster list is compacted in order, until one cluster is left. Merging by
+// box area tracks SAH quality far more closely than Morton splits on scenes
+// of overlapping or very unevenly sized triangles.
+// LBVH, Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees,
+// and k-d Trees" (HPG 2012): one thread per internal node finds its key range
+// and split; bounds propagate bottom-up (the second child to arrive merges).
+// Output: subtrees of <= kLeafMax triangles collapse into leaves; each inner
+// node is a 64-byte Node2 holding both children's boxes (root at index 0); the
+// triangle vertices are gathered into leaf order (48 B per triangle).
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
 
 #include "xgb_kernels.h"
 
@@ -199,6 +208,133 @@ __global__ void k_gather(const unsigned int* __restrict__ vals, int n, const flo
     tris[k] = tv;
 }
 
+// ---- PLOC -------------------------------------------------------------------
+// Node ids: leaf k (k-th triangle in Morton order) is k; internal nodes are
+// n .. 2n-2 in creation order (the root is created last). Output Node2 index of
+// internal node id is (2n-2) - id, so the root lands at 0.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__device__ __forceinline__ float halfArea(float4 lo, float4 hi) {
+    float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_plocInit(const unsigned int* __restrict__ vals, int n, const float4* __restrict__ triLo,
+                           const float4* __restrict__ triHi, float4* nodeLo, float4* nodeHi, int* clusters, int* count,
+                           int* parent) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned int t = vals[k];
+    nodeLo[k] = triLo[t];
+    nodeHi[k] = triHi[t];
+    clusters[k] = k;
+    count[k] = 1;
+    parent[k] = -1;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_plocNearest(const int* __restrict__ clusters, int nc,
+                                                            const float4* __restrict__ nodeLo,
+                                                            const float4* __restrict__ nodeHi, int* nn) {
+    __shared__ float4 sLo[kPlocBlock + 2 * kPlocRadius], sHi[kPlocBlock + 2 * kPlocRadius];
+    const int b0 = blockIdx.x * kPlocBlock;
+    for (int t = threadIdx.x; t < kPlocBlock + 2 * kPlocRadius; t += kPlocBlock) {
+        int j = b0 - kPlocRadius + t;
+        if (j >= 0 && j < nc) {
+            int id = clusters[j];
+            sLo[t] = nodeLo[id];
+            sHi[t] = nodeHi[id];
+        }
+    }
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
+    if (i >= nc) return;
+    const int si = threadIdx.x + kPlocRadius;
+    const float4 lo = sLo[si], hi = sHi[si];
+    float best = __int_as_float(0x7f800000);
+    int bestJ = -1;
+    const int jLo = max(0, i - kPlocRadius), jHi = min(nc - 1, i + kPlocRadius);
+    for (int j = jLo; j <= jHi; ++j) {
+        if (j == i) continue;
+        const float4 l2 = sLo[j - b0 + kPlocRadius], h2 = sHi[j - b0 + kPlocRadius];
+        float a = halfArea(make_float4(fminf(lo.x, l2.x), fminf(lo.y, l2.y), fminf(lo.z, l2.z), 0.f),
+                           make_float4(fmaxf(hi.x, h2.x), fmaxf(hi.y, h2.y), fmaxf(hi.z, h2.z), 0.f));
+        if (a < best || bestJ < 0) { best = a; bestJ = j; }  // ascending j: ties go to the lower index
+    }
+    nn[i] = bestJ;
+}
+
+__global__ void k_plocMerge(int* clusters, int nc, const int* __restrict__ nn, int n, float4* nodeLo, float4* nodeHi,
+                            int* left, int* right, int* parent, int* count, int* counter, int* keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nc) return;
+    const int j = nn[i];
+    const bool mutual = j >= 0 && nn[j] == i;
+    if (mutual && i < j) {
+        const int a = clusters[i], b = clusters[j];
+        const int id = n + atomicAdd(counter, 1);
+        const float4 al = nodeLo[a], ah = nodeHi[a], bl = nodeLo[b], bh = nodeHi[b];
+        nodeLo[id] = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
+        nodeHi[id] = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+        left[id - n] = a;
+        right[id - n] = b;
+        parent[a] = id;
+        parent[b] = id;
+        parent[id] = -1;
+        count[id] = count[a] + count[b];
+        clusters[i] = id;  // only this thread touches slot i; slot j is dropped by its own thread
+        keep[i] = 1;
+    } else {
+        keep[i] = mutual ? 0 : 1;
+    }
+}
+
+// Position of every node's first triangle in depth-first (left before right) order.
+__global__ void k_dfsOffset(int nNodes, int n, const int* __restrict__ parent, const int* __restrict__ left,
+                            const int* __restrict__ right, const int* __restrict__ count, int* dfs) {
+    const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x0 >= nNodes) return;
+    int off = 0, x = x0;
+    for (int p = parent[x]; p >= 0; x = p, p = parent[x])
+        if (right[p - n] == x) off += count[left[p - n]];
+    dfs[x0] = off;
+}
+
+__device__ __forceinline__ int plocChild(int c, int n, const int* count, const int* dfs) {
+    const int cnt = count[c];
+    if (cnt <= kLeafMax) return leafEncode(dfs[c], cnt);
+    return (2 * n - 2) - c;
+}
+
+__global__ void k_plocEmit(int n, const int* __restrict__ left, const int* __restrict__ right,
+                           const int* __restrict__ count, const int* __restrict__ dfs, const float4* __restrict__ nodeLo,
+                           const float4* __restrict__ nodeHi, Node2* nodes) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n - 1) return;
+    const int id = n + k;
+    const int a = left[k], b = right[k];
+    const float4 al = nodeLo[a], ah = nodeHi[a], bl = nodeLo[b], bh = nodeHi[b];
+    Node2 nd;
+    nd.a = make_float4(al.x, al.y, al.z, ah.x);
+    nd.b = make_float4(ah.y, ah.z, bl.x, bl.y);
+    nd.c = make_float4(bl.z, bh.x, bh.y, bh.z);
+    nd.d = make_int4(plocChild(a, n, count, dfs), plocChild(b, n, count, dfs), 0, 0);
+    nodes[(2 * n - 2) - id] = nd;
+}
+
+__global__ void k_plocGather(const unsigned int* __restrict__ vals, int n, const int* __restrict__ dfs,
+                             const float4* __restrict__ pos, const int* __restrict__ idx, TriV* tris) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int t = (int)vals[k];
+    const float4 a = pos[idx[3 * t]], b = pos[idx[3 * t + 1]], c = pos[idx[3 * t + 2]];
+    TriV tv;
+    tv.p0 = make_float4(a.x, a.y, a.z, __int_as_float(t));
+    tv.p1 = make_float4(b.x, b.y, b.z, 0.0f);
+    tv.p2 = make_float4(c.x, c.y, c.z, 0.0f);
+    tris[dfs[k]] = tv;
+}
+
 struct DeviceScratch {
     void* p = nullptr;
     ~DeviceScratch() { if (p) cudaFree(p); }
@@ -226,6 +362,15 @@ cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream
     size_t oParent = take(4 * nNodes), oArr = take(4 * (size_t)n);
     size_t oNLo = take(sizeof(float4) * nNodes), oNHi = take(sizeof(float4) * nNodes);
     size_t oSort = take(sortTemp);
+    // PLOC: second cluster list, nearest neighbours, keep flags, counts, DFS offsets, counters, select scratch
+    const bool ploc = in.builder == kBuilderPloc;
+    size_t selTemp = 0;
+    if (ploc)
+        cub::DeviceSelect::Flagged(nullptr, selTemp, (int*)nullptr, (int*)nullptr, (int*)nullptr, (int*)nullptr, n, stream);
+    size_t oClB = ploc ? take(4 * (size_t)n) : 0, oNN = ploc ? take(4 * (size_t)n) : 0;
+    size_t oKeep = ploc ? take(4 * (size_t)n) : 0, oCount = ploc ? take(4 * nNodes) : 0;
+    size_t oDfs = ploc ? take(4 * nNodes) : 0, oCounters = ploc ? take(16) : 0;
+    size_t oSel = ploc ? take(selTemp) : 0;
     DeviceScratch scratch;
     if ((e = cudaMalloc(&scratch.p, off)) != cudaSuccess) return e;
     char* base = (char*)scratch.p;
@@ -247,15 +392,49 @@ cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream
     k_morton<<<G, B, 0, stream>>>(cent, n, bounds, keys, vals);
     if ((e = cub::DeviceRadixSort::SortPairs(base + oSort, sortTemp, keys, keys2, vals, vals2, n, 0, 30, stream)) != cudaSuccess)
         return e;
-    if (n >= 2) {
-        int Gi = (n - 1 + B - 1) / B;
-        if ((e = cudaMemsetAsync(arrivals, 0, 4 * (size_t)n, stream)) != cudaSuccess) return e;
-        k_karras<<<Gi, B, 0, stream>>>(keys2, n, left, right, first, last, parent);
-        k_leafBoxes<<<G, B, 0, stream>>>(vals2, n, triLo, triHi, nodeLo, nodeHi);
-        k_bottomUp<<<G, B, 0, stream>>>(n, parent, left, right, nodeLo, nodeHi, arrivals);
-        k_emit<<<Gi, B, 0, stream>>>(n, left, right, first, last, nodeLo, nodeHi, out->nodes);
+    if (ploc) {
+        int* clA = (int*)(base + oKeys);  // the unsorted keys are free once sorted
+        int* clB = (int*)(base + oClB);
+        int* nn = (int*)(base + oNN);
+        int* keep = (int*)(base + oKeep);
+        int* count = (int*)(base + oCount);
+        int* dfs = (int*)(base + oDfs);
+        int* counters = (int*)(base + oCounters);  // [0] nodes created, [1] clusters selected
+        if ((e = cudaMemsetAsync(counters, 0, 16, stream)) != cudaSuccess) return e;
+        k_plocInit<<<G, B, 0, stream>>>(vals2, n, triLo, triHi, nodeLo, nodeHi, clA, count, parent);
+        int nc = n;
+        int* hostCount = nullptr;
+        if ((e = cudaMallocHost((void**)&hostCount, 4)) != cudaSuccess) return e;
+        for (int round = 0; nc > 1; ++round) {
+            if (round > 4 * 1024) { cudaFreeHost(hostCount); return cudaErrorUnknown; }  // cannot happen: a round merges >= 1 pair
+            const int Gc = (nc + kPlocBlock - 1) / kPlocBlock;
+            k_plocNearest<<<Gc, kPlocBlock, 0, stream>>>(clA, nc, nodeLo, nodeHi, nn);
+            k_plocMerge<<<Gc, kPlocBlock, 0, stream>>>(clA, nc, nn, n, nodeLo, nodeHi, left, right, parent, count,
+                                                        counters, keep);
+            size_t tb = selTemp;
+            if ((e = cub::DeviceSelect::Flagged(base + oSel, tb, clA, keep, clB, counters + 1, nc, stream)) != cudaSuccess) break;
+            if ((e = cudaMemcpyAsync(hostCount, counters + 1, 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) break;
+            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) break;
+            nc = *hostCount;
+            std::swap(clA, clB);
+        }
+        cudaFreeHost(hostCount);
+        if (e != cudaSuccess) return e;
+        const int nAll = 2 * n - 1;
+        k_dfsOffset<<<(nAll + B - 1) / B, B, 0, stream>>>(nAll, n, parent, left, right, count, dfs);
+        if (n >= 2) k_plocEmit<<<(n - 1 + B - 1) / B, B, 0, stream>>>(n, left, right, count, dfs, nodeLo, nodeHi, out->nodes);
+        k_plocGather<<<G, B, 0, stream>>>(vals2, n, dfs, in.pos, in.idx, out->tris);
+    } else {
+        if (n >= 2) {
+            int Gi = (n - 1 + B - 1) / B;
+            if ((e = cudaMemsetAsync(arrivals, 0, 4 * (size_t)n, stream)) != cudaSuccess) return e;
+            k_karras<<<Gi, B, 0, stream>>>(keys2, n, left, right, first, last, parent);
+            k_leafBoxes<<<G, B, 0, stream>>>(vals2, n, triLo, triHi, nodeLo, nodeHi);
+            k_bottomUp<<<G, B, 0, stream>>>(n, parent, left, right, nodeLo, nodeHi, arrivals);
+            k_emit<<<Gi, B, 0, stream>>>(n, left, right, first, last, nodeLo, nodeHi, out->nodes);
+        }
+        k_gather<<<G, B, 0, stream>>>(vals2, n, in.pos, in.idx, out->tris);
     }
-    k_gather<<<G, B, 0, stream>>>(vals2, n, in.pos, in.idx, out->tris);
     unsigned int hb[12];
     if ((e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;

@@ -257,6 +257,28 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat(SceneDev sc, RenderP
         atomicAdd(ANY ? &ctrl->shadowRays : &ctrl->extensionRays, (unsigned long long)n);
 }
 
+// ---- ray queries (xgb_scene_intersect / xgb_scene_occluded) -------------------
+__global__ void __launch_bounds__(kTraceBlock) k_query(SceneDev sc, const float4* o, const float4* d, int n, int any,
+                                                       float4* hits, int* occluded, unsigned int* errors) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 oo = o[i], dd = d[i];
+        TraceHit hit;
+        WorkCount wc;
+        if (any) {
+            occluded[i] = traceScene<true>(sc, V3(oo.x, oo.y, oo.z), V3(dd.x, dd.y, dd.z), oo.w, hit, errors, wc) ? 1 : 0;
+        } else {
+            traceScene<false>(sc, V3(oo.x, oo.y, oo.z), V3(dd.x, dd.y, dd.z), oo.w, hit, errors, wc);
+            hits[2 * i] = make_float4(hit.t, __int_as_float(hit.inst), __int_as_float(hit.prim), 0.0f);
+            hits[2 * i + 1] = make_float4(hit.b0, hit.b1, 0.0f, 0.0f);
+        }
+    }
+}
+
+void launchQuery(const SceneDev& sc, const float4* o, const float4* d, int n, int any, float4* hits, int* occluded,
+                 unsigned int* errors, int grid, cudaStream_t s) {
+    k_query<<<grid, kTraceBlock, 0, s>>>(sc, o, d, n, any, hits, occluded, errors);
+}
+
 static int g_extendBlocks = 0, g_shadowBlocks = 0;
 
 int extendBlocksPerSM() {

@@ -9,10 +9,13 @@
 namespace xgb {
 
 // ---- BVH build (bvh_build.cu) ------------------------------------------------
+constexpr int kBuilderPloc = 0;  // locally-ordered clustering (default)
+constexpr int kBuilderLbvh = 1;  // Morton-split linear BVH
 struct BlasBuildInput {
     const float4* pos;  // device, object space
     const int* idx;     // device, 3 per triangle
     int nTris;
+    int builder;        // kBuilderPloc or kBuilderLbvh
 };
 struct BlasBuildOutput {
     Node2* nodes;       // device, nTris - 1 entries (nTris >= 2)
@@ -23,7 +26,7 @@ struct BlasBuildOutput {
     int rootLeaf;
     float boundsLo[3], boundsHi[3];  // object-space bounds of the vertices used
 };
-// Builds a binary LBVH over the triangles on `stream` and synchronises it.
+// Builds a binary BVH over the triangles on `stream` and synchronises it.
 // Returns a CUDA error code (cudaSuccess on success).
 cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream_t stream);
 
@@ -123,6 +126,10 @@ void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQu
                  Ctrl* ctrl, int grid, cudaStream_t s);
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int grid,
                   cudaStream_t s);
+// Ray queries on a built scene: rays o (xyz, w = tMax) and d; closest hits as 2 float4
+// per ray (t, bits(instance), bits(triangle), -; b0, b1, -, -) or any-hit flags.
+void launchQuery(const SceneDev& sc, const float4* o, const float4* d, int n, int any, float4* hits, int* occluded,
+                 unsigned int* errors, int grid, cudaStream_t s);
 int extendBlocksPerSM();
 int shadowBlocksPerSM();
 

@@ -135,6 +135,16 @@ class SceneDesc:
     def n_paths(self) -> int:
         return self.width * self.height * self.spp
 
+    def bounds(self):
+        """World-space box (lo, hi) of every object's vertices (float64)."""
+        lo, hi = np.full(3, np.inf), np.full(3, -np.inf)
+        for o in self.objects:
+            p = self.meshes[o.mesh].pos.astype(np.float64)
+            m = np.asarray(o.transform.mat, np.float64).reshape(4, 4)
+            w = p @ m[:3, :3].T + m[:3, 3]
+            lo, hi = np.minimum(lo, w.min(axis=0)), np.maximum(hi, w.max(axis=0))
+        return lo, hi
+
     # -- replay ----------------------------------------------------------------
     def emit(self, backend):
         """Replay into a backend exposing add_texture / add_mesh / add_material /
