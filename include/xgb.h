@@ -50,6 +50,12 @@ xgb_status xgb_ctx_destroy(xgb_ctx* ctx);
 #define XGB_BVH_PLOC 0
 #define XGB_BVH_LBVH 1
 xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder);
+/* Node layout of the per-mesh BVH for meshes created afterwards: XGB_BVH_BINARY
+ * (default; 64-byte nodes with two float boxes) or XGB_BVH_WIDE8 (80-byte nodes
+ * with eight 8-bit quantised boxes, leaves of up to 3 triangles). */
+#define XGB_BVH_BINARY 0
+#define XGB_BVH_WIDE8 1
+xgb_status xgb_ctx_set_bvh_layout(xgb_ctx* ctx, int layout);
 /* Waits for the work enqueued on stream (NULL = the context's own stream). */
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream);
 /* Last error message of this context ("" when none). Never NULL. */

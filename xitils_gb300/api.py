@@ -63,6 +63,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_ctx_destroy": [P],
         "xgb_ctx_synchronize": [P, P],
         "xgb_ctx_set_bvh_builder": [P, C.c_int],
+        "xgb_ctx_set_bvh_layout": [P, C.c_int],
         "xgb_scene_intersect": [P, C.c_int, FP, FP, P],
         "xgb_scene_occluded": [P, C.c_int, FP, C.POINTER(C.c_int32), P],
         "xgb_film_enable_aovs": [P],
@@ -165,6 +166,12 @@ class Context:
     def set_bvh_builder(self, name: str):
         """BVH builder for meshes created afterwards: "ploc" (default) or "lbvh"."""
         self.check(self.lib.xgb_ctx_set_bvh_builder(self.h, self.BVH_BUILDERS[name]), "set_bvh_builder")
+
+    BVH_LAYOUTS = {"binary": 0, "wide8": 1}
+
+    def set_bvh_layout(self, name: str):
+        """Node layout of the BVH of meshes created afterwards: "binary" (default) or "wide8"."""
+        self.check(self.lib.xgb_ctx_set_bvh_layout(self.h, self.BVH_LAYOUTS[name]), "set_bvh_layout")
 
     def synchronize(self, stream=None):
         self.check(self.lib.xgb_ctx_synchronize(self.h, stream), "synchronize")

@@ -93,6 +93,7 @@ struct xgb_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     int bvhBuilder = kBuilderPloc;
+    int bvhLayout = kLayoutBinary;
 };
 
 struct xgb_texture {
@@ -111,7 +112,9 @@ struct xgb_mesh {
     float2* dUV = nullptr;
     int* dIdx = nullptr;
     float* dArea = nullptr;
-    Node2* dNodes = nullptr;
+    WNode* dNodes = nullptr;   // 8-wide BVH (allocated by buildBlas)
+    Node2* dNodes2 = nullptr;  // binary BVH (allocated by buildBlas)
+    int wide = 0;
     TriV* dTris = nullptr;
     int rootIsLeaf = 1, rootLeaf = 0;
     std::vector<float> triArea;  // TriangleIndexed::surfaceArea
@@ -250,6 +253,14 @@ xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder) {
     return XGB_OK;
 }
 
+xgb_status xgb_ctx_set_bvh_layout(xgb_ctx* ctx, int layout) {
+    if (!ctx) return XGB_INVALID_ARG;
+    if (layout != XGB_BVH_BINARY && layout != XGB_BVH_WIDE8)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_bvh_layout: unknown layout");
+    ctx->bvhLayout = layout == XGB_BVH_WIDE8 ? kLayoutWide : kLayoutBinary;
+    return XGB_OK;
+}
+
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream) {
     if (!ctx) return XGB_INVALID_ARG;
     XGB_CUDA(ctx, cudaStreamSynchronize(pick(ctx, stream)));
@@ -291,7 +302,7 @@ xgb_status xgb_texture_destroy(xgb_texture* tex) {
 static void freeMesh(xgb_mesh* m) {
     for (const void* p : {(const void*)m->dPos, (const void*)m->dNrm, (const void*)m->dTan, (const void*)m->dBit,
                           (const void*)m->dGnrm, (const void*)m->dUV, (const void*)m->dIdx, (const void*)m->dArea,
-                          (const void*)m->dNodes, (const void*)m->dTris})
+                          (const void*)m->dNodes, (const void*)m->dNodes2, (const void*)m->dTris})
         dfree(p);
 }
 
@@ -362,12 +373,14 @@ xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* position
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->dGnrm, sizeof(float4) * m->nTris);
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->dArea, sizeof(float) * m->nTris);
     if (e == cudaSuccess) e = cudaMalloc((void**)&m->dTris, sizeof(TriV) * m->nTris);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&m->dNodes, sizeof(Node2) * std::max(1, m->nTris - 1));
     if (e == cudaSuccess) {
-        BlasBuildInput in{m->dPos, m->dIdx, m->nTris, ctx->bvhBuilder};
+        BlasBuildInput in{m->dPos, m->dIdx, m->nTris, ctx->bvhBuilder, ctx->bvhLayout};
         BlasBuildOutput o{};
-        o.nodes = m->dNodes; o.tris = m->dTris; o.gnrm = m->dGnrm; o.triArea = m->dArea;
+        o.tris = m->dTris; o.gnrm = m->dGnrm; o.triArea = m->dArea;
         e = buildBlas(in, &o, s);
+        m->dNodes = o.nodes;
+        m->dNodes2 = o.nodes2;
+        m->wide = o.wide;
         m->rootIsLeaf = o.rootIsLeaf;
         m->rootLeaf = o.rootLeaf;
     }
@@ -724,11 +737,14 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     std::vector<TextureDev> td(texs.size());
     for (size_t i = 0; i < texs.size(); ++i) td[i] = TextureDev{texs[i]->d, texs[i]->w, texs[i]->h, texs[i]->clamp, texs[i]->filter};
     std::vector<MeshDev> md(meshes.size());
+    int nWideMeshes = 0;
     for (size_t i = 0; i < meshes.size(); ++i) {
         const xgb_mesh* m = meshes[i];
-        md[i] = MeshDev{m->dNodes, m->dTris, m->dPos, m->dUV, m->dNrm, m->dTan, m->dBit, m->dIdx, m->dGnrm, m->dArea,
-                        m->nTris, m->nV, m->rootIsLeaf, m->rootLeaf};
+        md[i] = MeshDev{m->dNodes2, m->dNodes, m->wide, m->dTris, m->dPos, m->dUV, m->dNrm, m->dTan, m->dBit, m->dIdx,
+                        m->dGnrm, m->dArea, m->nTris, m->nV, m->rootIsLeaf, m->rootLeaf};
+        nWideMeshes += m->wide;
     }
+    const int blasLayout = nWideMeshes == 0 ? 0 : (nWideMeshes == (int)meshes.size() ? 1 : 2);
 
     // lights (Scene.h:17-22) and their sampling constants
     std::vector<LightDev> lights;
@@ -809,6 +825,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.tlas = dTlas;
     sd.nInstances = (int)inst.size();
     sd.tlasRootIsLeaf = tlasRootIsLeaf;
+    sd.blasLayout = blasLayout;
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;
@@ -1045,8 +1062,6 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     init.totalPaths = total;
     *s->ctrlHost = init;
     XGB_CUDA(ctx, cudaMemcpyAsync(s->ctrl, s->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, st));
-    const int gTrace = ctx->numSMs * extendBlocksPerSM();
-    const int gShadow = ctx->numSMs * shadowBlocksPerSM();
     const int gShade = ctx->numSMs * 8;
     int parity = 0;
     const int kIterPerCheck = 8;
@@ -1070,7 +1085,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
             if (prof) cudaEventRecord(ev[1], st);
             launchGenerate(s->sd, rp, X, s->ctrl, gShade, st);
             if (prof) cudaEventRecord(ev[2], st);
-            launchExtend(s->sd, X, s->rb.hits, s->ctrl, gTrace, prof, st);
+            launchExtend(s->sd, X, s->rb.hits, s->ctrl, ctx->numSMs, prof, st);
             if (gd) {
                 guideInferPaths(s->sd, gd->g, gb, X, s->rb.hits, s->ctrl, s->mix, gShade, st);
                 ++launches;
@@ -1078,7 +1093,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
             if (prof) cudaEventRecord(ev[3], st);
             launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, gShade, st);
             if (prof) cudaEventRecord(ev[4], st);
-            launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, gShadow, st);
+            launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, ctx->numSMs, st);
             if (prof) cudaEventRecord(ev[5], st);
             launches += 5;
             parity ^= 1;

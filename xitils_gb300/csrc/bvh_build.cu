@@ -16,9 +16,13 @@
 // LBVH, Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees,
 // and k-d Trees" (HPG 2012): one thread per internal node finds its key range
 // and split; bounds propagate bottom-up (the second child to arrive merges).
-// Output: subtrees of <= kLeafMax triangles collapse into leaves; each inner
-// node is a 64-byte Node2 holding both children's boxes (root at index 0); the
-// triangle vertices are gathered into leaf order (48 B per triangle).
+// Output: the binary tree becomes an 8-wide compressed BVH (WNode, xgb_types.h),
+// top down, one round per level: a wide node takes a binary node's two
+// children and keeps opening the child of largest surface area until it has
+// eight (subtrees of <= kWideLeafMax triangles may stay closed as leaf
+// children), assigns them to slots by direction octant, quantises their boxes
+// to 8 bits against its own box (rounded outwards), and gathers the leaf
+// children's triangles next to each other (48 B per triangle).
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_select.cuh>
 
@@ -335,6 +339,177 @@ __global__ void k_plocGather(const unsigned int* __restrict__ vals, int n, const
     tris[dfs[k]] = tv;
 }
 
+// ---- LBVH -> the PLOC numbering used by the wide conversion ----------------------
+// LBVH internal node i becomes n + i (root n), leaf n - 1 + k becomes k.
+__global__ void k_lbvhUnify(int n, const int* __restrict__ left, const int* __restrict__ right,
+                            const int* __restrict__ first, const int* __restrict__ last,
+                            const float4* __restrict__ nodeLo, const float4* __restrict__ nodeHi, int* uLeft, int* uRight,
+                            int* uCount, int* uStart, float4* uLo, float4* uHi) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 2 * n - 1) return;
+    if (x < n) {  // leaf x (LBVH id n - 1 + x)
+        uCount[x] = 1;
+        uStart[x] = x;
+        uLo[x] = nodeLo[n - 1 + x];
+        uHi[x] = nodeHi[n - 1 + x];
+    } else {  // internal n + i (LBVH id i)
+        const int i = x - n;
+        auto map = [n](int c) { return c >= n - 1 ? c - (n - 1) : n + c; };
+        uLeft[i] = map(left[i]);
+        uRight[i] = map(right[i]);
+        uCount[x] = last[i] - first[i] + 1;
+        uStart[x] = first[i];
+        uLo[x] = nodeLo[i];
+        uHi[x] = nodeHi[i];
+    }
+}
+
+// ---- binary -> 8-wide compressed BVH ------------------------------------------
+struct WideItem {
+    int bin;   // binary node id (PLOC numbering)
+    int wide;  // WNode index it becomes
+};
+
+struct WideBuild {
+    const int* left;   // [id - n] for internal ids
+    const int* right;
+    const int* count;  // triangles under each node
+    const int* start;  // first triangle of each node in the binary-order triangle array
+    const float4* lo;
+    const float4* hi;
+    const TriV* trisIn;  // binary (leaf) order
+    int n;
+    WNode* nodes;
+    int nodeCap;
+    TriV* trisOut;
+    int* counters;  // [0] wide nodes used, [1] triangles placed, [2] items written, [3] error
+};
+
+__device__ __forceinline__ int wideExponent(float lo, float hi) {
+    const float ext = __fsub_ru(hi, lo);
+    if (!(ext > 0.0f)) return 1;  // flat axis: the smallest normal scale
+    int x;
+    frexpf(ext / 255.0f, &x);
+    int e = x - 1;
+    while (e < 127 && ldexpf(255.0f, e) < ext) ++e;
+    while (e > -126 && ldexpf(255.0f, e - 1) >= ext) --e;
+    return min(max(e, -126), 127) + 127;  // biased: 1 .. 254
+}
+
+__device__ __forceinline__ unsigned int quantLo(float c, float p, int eb) {
+    double q = floor(((double)c - (double)p) * ldexp(1.0, 127 - eb)) - 1.0;  // one step outwards
+    return (unsigned int)fmin(fmax(q, 0.0), 255.0);
+}
+__device__ __forceinline__ unsigned int quantHi(float c, float p, int eb) {
+    double q = ceil(((double)c - (double)p) * ldexp(1.0, 127 - eb)) + 1.0;
+    return (unsigned int)fmin(fmax(q, 0.0), 255.0);
+}
+
+__global__ void k_wideRound(WideBuild wb, const WideItem* in, int nIn, WideItem* out) {
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nIn) return;
+    const int n = wb.n;
+    const WideItem item = in[it];
+    // children: open the largest-area inner child until there are eight
+    int ch[8];
+    int nch = 2;
+    ch[0] = wb.left[item.bin - n];
+    ch[1] = wb.right[item.bin - n];
+    while (nch < 8) {
+        int best = -1;
+        float bestA = -1.0f;
+        for (int j = 0; j < nch; ++j) {
+            if (wb.count[ch[j]] < 2) continue;  // a single triangle cannot be opened
+            float a = halfArea(wb.lo[ch[j]], wb.hi[ch[j]]);
+            // subtrees too big for a leaf child must be opened or become wide nodes: prefer them on ties
+            if (a > bestA || (a == bestA && wb.count[ch[j]] > kWideLeafMax)) { bestA = a; best = j; }
+        }
+        if (best < 0) break;
+        const int c = ch[best];
+        ch[best] = wb.left[c - n];
+        ch[nch++] = wb.right[c - n];
+    }
+    // slot assignment: slot s takes the child furthest towards -dir(s), where bit k of
+    // s set means a negative k component; greedy over the 8 x 8 costs
+    const float4 plo = wb.lo[item.bin], phi = wb.hi[item.bin];
+    const float cx = 0.5f * (plo.x + phi.x), cy = 0.5f * (plo.y + phi.y), cz = 0.5f * (plo.z + phi.z);
+    int slotChild[8];
+    for (int s = 0; s < 8; ++s) slotChild[s] = -1;
+    unsigned int usedChild = 0, usedSlot = 0;
+    for (int round = 0; round < nch; ++round) {
+        float bestC = __int_as_float(0x7f800000);
+        int bj = -1, bs = -1;
+        for (int j = 0; j < nch; ++j) {
+            if (usedChild >> j & 1) continue;
+            const float4 l = wb.lo[ch[j]], h = wb.hi[ch[j]];
+            const float dx = 0.5f * (l.x + h.x) - cx, dy = 0.5f * (l.y + h.y) - cy, dz = 0.5f * (l.z + h.z) - cz;
+            for (int sl = 0; sl < 8; ++sl) {
+                if (usedSlot >> sl & 1) continue;
+                const float cost = ((sl & 1) ? -dx : dx) + ((sl & 2) ? -dy : dy) + ((sl & 4) ? -dz : dz);
+                if (cost < bestC || bj < 0) { bestC = cost; bj = j; bs = sl; }
+            }
+        }
+        usedChild |= 1u << bj;
+        usedSlot |= 1u << bs;
+        slotChild[bs] = ch[bj];
+    }
+    // allocation: inner children contiguous from childBase, leaf triangles from triBase
+    int nInner = 0, nTri = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int c = slotChild[s];
+        if (c < 0) continue;
+        if (wb.count[c] > kWideLeafMax) ++nInner;
+        else nTri += wb.count[c];
+    }
+    const int childBase = nInner ? atomicAdd(&wb.counters[0], nInner) : 0;
+    const int triBase = nTri ? atomicAdd(&wb.counters[1], nTri) : 0;
+    if (childBase + nInner > wb.nodeCap || triBase + nTri > n) {
+        atomicOr(&wb.counters[3], 1);
+        return;
+    }
+    const int outBase = nInner ? atomicAdd(&wb.counters[2], nInner) : 0;
+    // quantisation frame of this node
+    const int ex = wideExponent(plo.x, phi.x), ey = wideExponent(plo.y, phi.y), ez = wideExponent(plo.z, phi.z);
+    unsigned int imask = 0, meta[2] = {0, 0}, q[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int kInner = 0, off = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int c = slotChild[s];
+        unsigned int mb = 0;
+        const int w = s >> 2, sh = 8 * (s & 3);
+        if (c >= 0) {
+            const float4 l = wb.lo[c], h = wb.hi[c];
+            q[0 + w] |= quantLo(l.x, plo.x, ex) << sh;
+            q[2 + w] |= quantLo(l.y, plo.y, ey) << sh;
+            q[4 + w] |= quantLo(l.z, plo.z, ez) << sh;
+            q[6 + w] |= quantHi(h.x, plo.x, ex) << sh;
+            q[8 + w] |= quantHi(h.y, plo.y, ey) << sh;
+            q[10 + w] |= quantHi(h.z, plo.z, ez) << sh;
+            const int cnt = wb.count[c];
+            if (cnt > kWideLeafMax) {
+                imask |= 1u << s;
+                mb = (unsigned int)kInner;
+                out[outBase + kInner] = WideItem{c, childBase + kInner};
+                ++kInner;
+            } else {
+                mb = ((unsigned int)cnt << 5) | (unsigned int)off;
+                for (int k = 0; k < cnt; ++k) wb.trisOut[triBase + off + k] = wb.trisIn[wb.start[c] + k];
+                off += cnt;
+            }
+        } else {
+            // empty slot: an inverted box that no slab test accepts
+            q[0 + w] |= 255u << sh; q[2 + w] |= 255u << sh; q[4 + w] |= 255u << sh;
+        }
+        meta[w] |= mb << sh;
+    }
+    WNode nd;
+    nd.a = make_float4(plo.x, plo.y, plo.z, __uint_as_float((unsigned)ex | ((unsigned)ey << 8) | ((unsigned)ez << 16) | (imask << 24)));
+    nd.b = make_float4(__int_as_float(childBase), __int_as_float(triBase), __uint_as_float(meta[0]), __uint_as_float(meta[1]));
+    nd.c = make_float4(__uint_as_float(q[0]), __uint_as_float(q[1]), __uint_as_float(q[2]), __uint_as_float(q[3]));
+    nd.d = make_float4(__uint_as_float(q[4]), __uint_as_float(q[5]), __uint_as_float(q[6]), __uint_as_float(q[7]));
+    nd.e = make_float4(__uint_as_float(q[8]), __uint_as_float(q[9]), __uint_as_float(q[10]), __uint_as_float(q[11]));
+    wb.nodes[item.wide] = nd;
+}
+
 struct DeviceScratch {
     void* p = nullptr;
     ~DeviceScratch() { if (p) cudaFree(p); }
@@ -345,32 +520,42 @@ struct DeviceScratch {
 cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream_t stream) {
     const int n = in.nTris;
     if (n <= 0) return cudaErrorInvalidValue;
+    if (n >= (1 << 24)) return cudaErrorInvalidValue;  // node indices travel in 24 bits on the traversal stack
+    out->nodes = nullptr;
+    out->nodes2 = nullptr;
+    out->nWide = 0;
+    const bool wide = in.layout == kLayoutWide;
+    out->wide = wide ? 1 : 0;
     const int B = 256;
     const int G = (n + B - 1) / B;
     cudaError_t e;
     // scratch layout
-    size_t nNodes = (size_t)2 * n - 1;
+    const size_t nNodes = (size_t)2 * n - 1;
     size_t sortTemp = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, sortTemp, (unsigned int*)nullptr, (unsigned int*)nullptr,
                                     (unsigned int*)nullptr, (unsigned int*)nullptr, n, 0, 30, stream);
+    size_t selTemp = 0;
+    cub::DeviceSelect::Flagged(nullptr, selTemp, (int*)nullptr, (int*)nullptr, (int*)nullptr, (int*)nullptr, n, stream);
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
-    size_t oTriLo = take(sizeof(float4) * n), oTriHi = take(sizeof(float4) * n), oCent = take(sizeof(float4) * n);
-    size_t oBounds = take(sizeof(unsigned int) * 12);
-    size_t oKeys = take(4 * (size_t)n), oVals = take(4 * (size_t)n), oKeys2 = take(4 * (size_t)n), oVals2 = take(4 * (size_t)n);
-    size_t oLeft = take(4 * (size_t)n), oRight = take(4 * (size_t)n), oFirst = take(4 * (size_t)n), oLast = take(4 * (size_t)n);
-    size_t oParent = take(4 * nNodes), oArr = take(4 * (size_t)n);
-    size_t oNLo = take(sizeof(float4) * nNodes), oNHi = take(sizeof(float4) * nNodes);
-    size_t oSort = take(sortTemp);
-    // PLOC: second cluster list, nearest neighbours, keep flags, counts, DFS offsets, counters, select scratch
-    const bool ploc = in.builder == kBuilderPloc;
-    size_t selTemp = 0;
-    if (ploc)
-        cub::DeviceSelect::Flagged(nullptr, selTemp, (int*)nullptr, (int*)nullptr, (int*)nullptr, (int*)nullptr, n, stream);
-    size_t oClB = ploc ? take(4 * (size_t)n) : 0, oNN = ploc ? take(4 * (size_t)n) : 0;
-    size_t oKeep = ploc ? take(4 * (size_t)n) : 0, oCount = ploc ? take(4 * nNodes) : 0;
-    size_t oDfs = ploc ? take(4 * nNodes) : 0, oCounters = ploc ? take(16) : 0;
-    size_t oSel = ploc ? take(selTemp) : 0;
+    const size_t oTriLo = take(sizeof(float4) * n), oTriHi = take(sizeof(float4) * n), oCent = take(sizeof(float4) * n);
+    const size_t oBounds = take(sizeof(unsigned int) * 12);
+    const size_t oKeys = take(4 * (size_t)n), oVals = take(4 * (size_t)n), oKeys2 = take(4 * (size_t)n),
+                 oVals2 = take(4 * (size_t)n);
+    const size_t oLeft = take(4 * (size_t)n), oRight = take(4 * (size_t)n), oFirst = take(4 * (size_t)n),
+                 oLast = take(4 * (size_t)n);
+    const size_t oParent = take(4 * nNodes), oArr = take(4 * (size_t)n);
+    const size_t oNLo = take(sizeof(float4) * nNodes), oNHi = take(sizeof(float4) * nNodes);
+    const size_t oSort = take(sortTemp);
+    const size_t oClB = take(4 * (size_t)n), oNN = take(4 * (size_t)n), oKeep = take(4 * (size_t)n);
+    const size_t oCount = take(4 * nNodes), oStart = take(4 * nNodes), oCounters = take(16), oSel = take(selTemp);
+    // unified (PLOC-numbered) tree for the wide conversion: LBVH writes its own copy
+    const size_t oULeft = take(4 * (size_t)n), oURight = take(4 * (size_t)n);
+    const size_t oULo = take(sizeof(float4) * nNodes), oUHi = take(sizeof(float4) * nNodes);
+    const size_t oTrisBin = take(sizeof(TriV) * n);
+    const size_t oItemsA = take(sizeof(WideItem) * n), oItemsB = take(sizeof(WideItem) * n);
+    const size_t oWide = take(sizeof(WNode) * n);  // upper bound: a wide node has >= 2 children
+    const size_t oWCounters = take(16);
     DeviceScratch scratch;
     if ((e = cudaMalloc(&scratch.p, off)) != cudaSuccess) return e;
     char* base = (char*)scratch.p;
@@ -384,6 +569,20 @@ cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream
         *last = (int*)(base + oLast), *parent = (int*)(base + oParent);
     unsigned int* arrivals = (unsigned int*)(base + oArr);
     float4 *nodeLo = (float4*)(base + oNLo), *nodeHi = (float4*)(base + oNHi);
+    int* count = (int*)(base + oCount);
+    int* start = (int*)(base + oStart);
+    TriV* trisBin = wide ? (TriV*)(base + oTrisBin) : out->tris;  // the binary layout gathers in place
+    Node2* nodes2 = nullptr;
+    if (!wide && n >= 2) {
+        if ((e = cudaMalloc((void**)&nodes2, sizeof(Node2) * (size_t)(n - 1))) != cudaSuccess) return e;
+        out->nodes2 = nodes2;  // the caller frees it, also on failure
+    }
+    int* hostCount = nullptr;
+    if ((e = cudaMallocHost((void**)&hostCount, 16)) != cudaSuccess) return e;
+    struct HostFree {
+        int* p;
+        ~HostFree() { cudaFreeHost(p); }
+    } hostFree{hostCount};
 
     unsigned int initBounds[12];
     for (int k = 0; k < 12; ++k) initBounds[k] = (k % 6) < 3 ? 0xFFFFFFFFu : 0u;
@@ -392,48 +591,95 @@ cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream
     k_morton<<<G, B, 0, stream>>>(cent, n, bounds, keys, vals);
     if ((e = cub::DeviceRadixSort::SortPairs(base + oSort, sortTemp, keys, keys2, vals, vals2, n, 0, 30, stream)) != cudaSuccess)
         return e;
-    if (ploc) {
+    // binary tree in the PLOC numbering: left/right/count/start/boxes, root id, triangles in leaf order
+    const int* uLeft = left;
+    const int* uRight = right;
+    const float4* uLo = nodeLo;
+    const float4* uHi = nodeHi;
+    int root = 2 * n - 2;
+    if (in.builder == kBuilderPloc) {
         int* clA = (int*)(base + oKeys);  // the unsorted keys are free once sorted
         int* clB = (int*)(base + oClB);
         int* nn = (int*)(base + oNN);
         int* keep = (int*)(base + oKeep);
-        int* count = (int*)(base + oCount);
-        int* dfs = (int*)(base + oDfs);
         int* counters = (int*)(base + oCounters);  // [0] nodes created, [1] clusters selected
         if ((e = cudaMemsetAsync(counters, 0, 16, stream)) != cudaSuccess) return e;
         k_plocInit<<<G, B, 0, stream>>>(vals2, n, triLo, triHi, nodeLo, nodeHi, clA, count, parent);
         int nc = n;
-        int* hostCount = nullptr;
-        if ((e = cudaMallocHost((void**)&hostCount, 4)) != cudaSuccess) return e;
         for (int round = 0; nc > 1; ++round) {
-            if (round > 4 * 1024) { cudaFreeHost(hostCount); return cudaErrorUnknown; }  // cannot happen: a round merges >= 1 pair
+            if (round > 4 * 1024) return cudaErrorUnknown;  // cannot happen: every round merges at least one pair
             const int Gc = (nc + kPlocBlock - 1) / kPlocBlock;
             k_plocNearest<<<Gc, kPlocBlock, 0, stream>>>(clA, nc, nodeLo, nodeHi, nn);
             k_plocMerge<<<Gc, kPlocBlock, 0, stream>>>(clA, nc, nn, n, nodeLo, nodeHi, left, right, parent, count,
                                                         counters, keep);
             size_t tb = selTemp;
-            if ((e = cub::DeviceSelect::Flagged(base + oSel, tb, clA, keep, clB, counters + 1, nc, stream)) != cudaSuccess) break;
-            if ((e = cudaMemcpyAsync(hostCount, counters + 1, 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) break;
-            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) break;
+            if ((e = cub::DeviceSelect::Flagged(base + oSel, tb, clA, keep, clB, counters + 1, nc, stream)) != cudaSuccess)
+                return e;
+            if ((e = cudaMemcpyAsync(hostCount, counters + 1, 4, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
             nc = *hostCount;
             std::swap(clA, clB);
         }
-        cudaFreeHost(hostCount);
-        if (e != cudaSuccess) return e;
         const int nAll = 2 * n - 1;
-        k_dfsOffset<<<(nAll + B - 1) / B, B, 0, stream>>>(nAll, n, parent, left, right, count, dfs);
-        if (n >= 2) k_plocEmit<<<(n - 1 + B - 1) / B, B, 0, stream>>>(n, left, right, count, dfs, nodeLo, nodeHi, out->nodes);
-        k_plocGather<<<G, B, 0, stream>>>(vals2, n, dfs, in.pos, in.idx, out->tris);
+        k_dfsOffset<<<(nAll + B - 1) / B, B, 0, stream>>>(nAll, n, parent, left, right, count, start);
+        if (!wide && n >= 2)
+            k_plocEmit<<<(n - 1 + B - 1) / B, B, 0, stream>>>(n, left, right, count, start, nodeLo, nodeHi, nodes2);
+        k_plocGather<<<G, B, 0, stream>>>(vals2, n, start, in.pos, in.idx, trisBin);
     } else {
         if (n >= 2) {
-            int Gi = (n - 1 + B - 1) / B;
+            const int Gi = (n - 1 + B - 1) / B;
             if ((e = cudaMemsetAsync(arrivals, 0, 4 * (size_t)n, stream)) != cudaSuccess) return e;
             k_karras<<<Gi, B, 0, stream>>>(keys2, n, left, right, first, last, parent);
             k_leafBoxes<<<G, B, 0, stream>>>(vals2, n, triLo, triHi, nodeLo, nodeHi);
             k_bottomUp<<<G, B, 0, stream>>>(n, parent, left, right, nodeLo, nodeHi, arrivals);
-            k_emit<<<Gi, B, 0, stream>>>(n, left, right, first, last, nodeLo, nodeHi, out->nodes);
+            if (!wide) k_emit<<<Gi, B, 0, stream>>>(n, left, right, first, last, nodeLo, nodeHi, nodes2);
+            int* ul = (int*)(base + oULeft);
+            int* ur = (int*)(base + oURight);
+            float4* ulo = (float4*)(base + oULo);
+            float4* uhi = (float4*)(base + oUHi);
+            k_lbvhUnify<<<((int)nNodes + B - 1) / B, B, 0, stream>>>(n, left, right, first, last, nodeLo, nodeHi, ul, ur,
+                                                                      count, start, ulo, uhi);
+            uLeft = ul; uRight = ur; uLo = ulo; uHi = uhi;
+            root = n;
         }
-        k_gather<<<G, B, 0, stream>>>(vals2, n, in.pos, in.idx, out->tris);
+        k_gather<<<G, B, 0, stream>>>(vals2, n, in.pos, in.idx, trisBin);
+    }
+    // binary -> 8-wide, one round per wide level
+    if (!wide) {
+        // binary layout: done (Node2 nodes emitted, triangles gathered in leaf order)
+    } else if (n <= kWideLeafMax) {
+        if ((e = cudaMemcpyAsync(out->tris, trisBin, sizeof(TriV) * n, cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
+            return e;
+    } else {
+        WideItem* itA = (WideItem*)(base + oItemsA);
+        WideItem* itB = (WideItem*)(base + oItemsB);
+        int* wc = (int*)(base + oWCounters);
+        const int init[4] = {1, 0, 0, 0};  // the root takes wide node 0
+        if ((e = cudaMemcpyAsync(wc, init, 16, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+        const WideItem rootItem{root, 0};
+        if ((e = cudaMemcpyAsync(itA, &rootItem, sizeof(WideItem), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+        WideBuild wb{uLeft, uRight, count, start, uLo, uHi, trisBin, n, (WNode*)(base + oWide), n, out->tris, wc};
+        int nIn = 1;
+        for (int level = 0; nIn > 0; ++level) {
+            if (level > 4096) return cudaErrorUnknown;  // cannot happen: every level goes one binary level deeper
+            if ((e = cudaMemsetAsync(wc + 2, 0, 4, stream)) != cudaSuccess) return e;
+            k_wideRound<<<(nIn + 127) / 128, 128, 0, stream>>>(wb, itA, nIn, itB);
+            if ((e = cudaMemcpyAsync(hostCount, wc, 16, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
+            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+            if (hostCount[3]) return cudaErrorUnknown;  // capacity check failed (cannot happen for a valid tree)
+            nIn = hostCount[2];
+            std::swap(itA, itB);
+        }
+        const int nWide = hostCount[0];
+        if (hostCount[1] != n) return cudaErrorUnknown;  // every triangle lands in exactly one leaf child
+        WNode* nodes = nullptr;
+        if ((e = cudaMalloc((void**)&nodes, sizeof(WNode) * nWide)) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(nodes, base + oWide, sizeof(WNode) * nWide, cudaMemcpyDeviceToDevice, stream)) != cudaSuccess) {
+            cudaFree(nodes);
+            return e;
+        }
+        out->nodes = nodes;
+        out->nWide = nWide;
     }
     unsigned int hb[12];
     if ((e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
@@ -443,8 +689,9 @@ cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream
         out->boundsLo[k] = orderedFloat(hb[6 + k]);
         out->boundsHi[k] = orderedFloat(hb[9 + k]);
     }
-    out->rootIsLeaf = n <= kLeafMax ? 1 : 0;
-    out->rootLeaf = leafEncode(0, n <= kLeafMax ? n : 1);
+    const int rootMax = wide ? kWideLeafMax : kLeafMax;
+    out->rootIsLeaf = n <= rootMax ? 1 : 0;
+    out->rootLeaf = leafEncode(0, n <= rootMax ? n : 1);
     return cudaSuccess;
 }
 

@@ -140,8 +140,6 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     std::memset(&host, 0, sizeof(host));
     host.totalPaths = total;
     if (cudaMemcpyAsync(ctrl, &host, sizeof(Ctrl), cudaMemcpyHostToDevice, st) != cudaSuccess) return XGB_CUDA_ERROR;
-    const int gTrace = numSMs * extendBlocksPerSM();
-    const int gShadow = numSMs * shadowBlocksPerSM();
     const int gShade = numSMs * 8;
     int parity = 0;
     for (int guard = 0;; ++guard) {
@@ -150,9 +148,9 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
             PathQueue& Y = q[parity ^ 1];
             launchPlan(ctrl, cap, st);
             launchGenerate(sd, rp, X, ctrl, gShade, st);
-            launchExtend(sd, X, hits, ctrl, gTrace, false, st);
+            launchExtend(sd, X, hits, ctrl, numSMs, false, st);
             launchShade(sd, rp, X, hits, Y, sq, ctrl, gShade, st);
-            launchShadow(sd, rp, sq, Y, ctrl, gShadow, st);
+            launchShadow(sd, rp, sq, Y, ctrl, numSMs, st);
             parity ^= 1;
         }
         if (cudaGetLastError() != cudaSuccess) return XGB_CUDA_ERROR;

@@ -3,6 +3,9 @@
 // Both are persistent: a grid of (SMs x resident blocks) threads where each
 // warp claims 32 queue entries at a time with one atomicAdd, so the grid drains
 // queues of any length without a relaunch per batch.
+#include <map>
+#include <mutex>
+
 #include "trace.cuh"
 #include "xgb_kernels.h"
 
@@ -92,7 +95,190 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(SceneDev sc, RenderParam
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctrl->shadowRays, (unsigned long long)n);
 }
 
-// ---- scenes of a few instances ------------------------------------------------
+// ---- scenes of a few instances: 8-wide mesh BVHs ------------------------------
+// With at most kFlatInstances instances the top level is a short list: a lane
+// walks the instances in order (those whose world box the ray still reaches
+// within tMax) and traverses each mesh's 8-wide BVH as a persistent per-lane
+// state machine in the style of Aila & Laine ("Understanding the Efficiency of
+// Ray Traversal on GPUs", HPG 2009): the lanes of a warp test nodes together
+// until each holds a leaf child (postponing it) or has no nodes left, then test
+// their leaves' triangles together; a lane whose ray is finished fetches the
+// next one at once (one atomicAdd per group of lanes), so the warp never waits
+// for its slowest ray. Results are those of traceScene: the same watertight
+// tests and the same closest-hit acceptance (tMax shrinks across instances).
+constexpr int kFlatInstances = 16;
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
+                                                            ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+    const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
+    unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
+    const int nInst = sc.nInstances;
+    const int lane = threadIdx.x & 31;
+    const unsigned int ltMask = (1u << lane) - 1u;
+    unsigned int stack[kWideStack];
+    int sp = 0;
+    int inst = nInst;  // instance being traversed
+    unsigned int ray = 0;
+    V3 wo(0.f, 0.f, 0.f), wd(0.f, 0.f, 1.f);
+    WRay r;
+    int oct = 0;
+    const WNode* nodes = nullptr;
+    const TriV* tris = nullptr;
+    WideHdr hd;
+    hd.imask = 0; hd.childBase = 0; hd.triBase = 0; hd.meta0 = 0; hd.meta1 = 0;
+    int node = 0;
+    unsigned int mask = 0;
+    bool inMesh = false;  // a mesh traversal is under way
+    int leafFirst = 0, leafCnt = 0;  // postponed leaf child
+    float tMax = 0.0f;
+    TraceHit hit;
+    hit.prim = -1;
+    hit.inst = -1;
+    hit.t = 0.0f;
+    hit.b0 = hit.b1 = 0.0f;
+    bool occluded = false;
+    bool fetch = true;
+    int steps = 0;  // traversal steps of the current ray
+    WorkCount wc;
+    for (;;) {
+        if (fetch) {
+            // lanes without a ray fetch the next ones together
+            const unsigned int act = __activemask();
+            const int leader = __ffs(act) - 1;
+            unsigned int base = 0;
+            if (lane == leader) base = atomicAdd(head, (unsigned int)__popc(act));
+            base = __shfl_sync(act, base, leader);
+            ray = base + __popc(act & ltMask);
+            if (ray >= n) break;
+            float4 o4, d4;
+            if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
+            else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
+            wo = V3(o4.x, o4.y, o4.z);
+            wd = V3(d4.x, d4.y, d4.z);
+            hit.prim = -1;
+            hit.inst = -1;
+            hit.t = tMax;
+            occluded = false;
+            inst = -1;
+            inMesh = false;
+            leafCnt = 0;
+            steps = 0;
+            fetch = false;
+        }
+        if (!inMesh) {
+            // next instance whose world box the ray still reaches, or the end of the ray
+            WRay wr = makeWRay(wo, wd);
+            if (!(ANY && occluded))
+                for (++inst; inst < nInst; ++inst) {
+                    float4 lo = __ldg(&sc.instBox[2 * inst]), hi = __ldg(&sc.instBox[2 * inst + 1]);
+                    float tn;
+                    if (slab(wr, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tMax, tn)) break;
+                }
+            if ((ANY && occluded) || inst >= nInst) {
+                if (ANY) {
+                    if (!occluded) {
+                        float4 cc = s.c[ray];
+                        filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
+                        int target = __float_as_int(cc.w);
+                        if (target >= 0) out.rng[target] = s.rng[ray];
+                        if (rp.train) creditPath(rp, s.pid[ray], cc);
+                    }
+                } else {
+                    h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
+                    h.inst[ray] = hit.inst;
+                }
+                fetch = true;
+            } else {
+                const Instance& in = sc.instances[inst];
+                const MeshDev& m = sc.meshes[in.mesh];
+                nodes = m.nodes;
+                tris = m.tris;
+                if (in.identity) r = wr;
+                else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
+                if (m.rootIsLeaf) {  // the whole mesh is one leaf: test it below, then the next instance
+                    leafFirst = 0;
+                    leafCnt = m.nTris;
+                } else {
+                    oct = rayOctant(r);
+                    sp = 0;
+                    node = 0;
+                    mask = wideEval(nodes, r, oct, tMax, hd);
+                    if (COUNT) wc.nodes++;
+                    inMesh = true;
+                }
+            }
+        }
+        // node phase: the warp steps through nodes until every lane holds a leaf child or has none left
+        for (;;) {
+            const bool active = inMesh && leafCnt == 0;
+            if (!__any_sync(__activemask(), active)) break;
+            if (!active) continue;
+            if (++steps > kMaxVisits) {
+                atomicOr(&ctrl->errors, 4u);
+                inMesh = false;
+                inst = nInst;
+                continue;
+            }
+            if (mask == 0u) {
+                if (sp == 0) {
+                    inMesh = false;  // this mesh is done
+                } else {
+                    const unsigned int e = stack[--sp];
+                    node = (int)(e >> 8);
+                    mask = e & 0xFFu;
+                    wideHeader(nodes + node, hd);
+                }
+                continue;
+            }
+            const int slot = (__ffs(mask) - 1) ^ oct;
+            mask &= mask - 1u;
+            const unsigned int mb = byteOf(slot >> 2 ? hd.meta1 : hd.meta0, slot);
+            if ((hd.imask >> slot) & 1u) {
+                if (mask) {
+                    if (sp >= kWideStack) {
+                        atomicOr(&ctrl->errors, 1u);
+                        inMesh = false;
+                        inst = nInst;
+                        continue;
+                    }
+                    stack[sp++] = ((unsigned int)node << 8) | mask;
+                }
+                node = hd.childBase + (int)mb;
+                mask = wideEval(nodes + node, r, oct, tMax, hd);
+                if (COUNT) wc.nodes++;
+            } else {
+                leafFirst = hd.triBase + (int)(mb & 31u);
+                leafCnt = (int)(mb >> 5);
+            }
+        }
+        // leaf phase: the postponed leaf children's triangles, together
+        if (leafCnt) {
+            if (COUNT) wc.tris += leafCnt;
+            if (testTris<ANY>(tris, leafFirst, leafCnt, r, tMax, hit, inst) && ANY) {
+                occluded = true;
+                inMesh = false;
+            }
+            leafCnt = 0;
+        }
+    }
+    if (COUNT) {
+        __syncwarp();  // every lane of the warp has left the loop
+        unsigned long long nv = wc.nodes, nt = wc.tris;
+        for (int off = 16; off > 0; off >>= 1) {
+            nv += __shfl_down_sync(0xFFFFFFFFu, nv, off);
+            nt += __shfl_down_sync(0xFFFFFFFFu, nt, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&ctrl->nodeVisits, nv);
+            atomicAdd(&ctrl->triTests, nt);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(ANY ? &ctrl->shadowRays : &ctrl->extensionRays, (unsigned long long)n);
+}
+
+// ---- scenes of a few instances: binary mesh BVHs ------------------------------------------------
 // With at most kFlatInstances instances the top level is a short list: a lane
 // walks the instances in order (those whose world box the ray still reaches
 // within tMax) and traverses each mesh BVH as a persistent per-lane state machine
@@ -104,10 +290,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(SceneDev sc, RenderParam
 // Results are those of traceScene: the same slab and watertight tests and the
 // same closest-hit acceptance (tMax shrinks across instances).
 constexpr int kSentinel = 0x7FFFFFFF;
-constexpr int kFlatInstances = 16;
 
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_flat(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
+__global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
                                                             ShadowQueue s, PathQueue out, Ctrl* ctrl) {
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
     unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
@@ -184,7 +369,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat(SceneDev sc, RenderP
             }
             const Instance& in = sc.instances[inst];
             const MeshDev& m = sc.meshes[in.mesh];
-            nodes = m.nodes;
+            nodes = m.nodes2;
             tris = m.tris;
             if (in.identity) r = wr;
             else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
@@ -243,10 +428,11 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat(SceneDev sc, RenderP
         }
     }
     if (COUNT) {
+        __syncwarp();  // every lane of the warp has left the loop
         unsigned long long nv = wc.nodes, nt = wc.tris;
         for (int off = 16; off > 0; off >>= 1) {
-            nv += __shfl_down_sync(__activemask(), nv, off);
-            nt += __shfl_down_sync(__activemask(), nt, off);
+            nv += __shfl_down_sync(0xFFFFFFFFu, nv, off);
+            nt += __shfl_down_sync(0xFFFFFFFFu, nt, off);
         }
         if (lane == 0) {
             atomicAdd(&ctrl->nodeVisits, nv);
@@ -279,34 +465,46 @@ void launchQuery(const SceneDev& sc, const float4* o, const float4* d, int n, in
     k_query<<<grid, kTraceBlock, 0, s>>>(sc, o, d, n, any, hits, occluded, errors);
 }
 
-static int g_extendBlocks = 0, g_shadowBlocks = 0;
 
-int extendBlocksPerSM() {
-    if (!g_extendBlocks) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_extendBlocks, k_extend<false>, kTraceBlock, 0);
-    return g_extendBlocks > 0 ? g_extendBlocks : 1;
-}
-int shadowBlocksPerSM() {
-    if (!g_shadowBlocks) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_shadowBlocks, k_shadow, kTraceBlock, 0);
-    return g_shadowBlocks > 0 ? g_shadowBlocks : 1;
+// Persistent grids: SMs x resident blocks of the kernel actually launched
+// (looked up once per kernel; all kernels here use kTraceBlock threads).
+template <class K>
+static int persistentGrid(K kernel, int numSMs) {
+    static std::mutex mu;
+    static std::map<const void*, int> blocks;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = blocks.find((const void*)kernel);
+    if (it == blocks.end()) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kTraceBlock, 0);
+        it = blocks.emplace((const void*)kernel, b > 0 ? b : 1).first;
+    }
+    return numSMs * it->second;
 }
 
-void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int grid, bool count, cudaStream_t s) {
+void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, bool count, cudaStream_t s) {
     RenderParams none{};
-    if (sc.nInstances <= kFlatInstances) {
-        if (count) k_trace_flat<false, true><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-        else k_trace_flat<false, false><<<grid, kTraceBlock, 0, s>>>(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-        return;
+    const bool flat = sc.nInstances <= kFlatInstances;
+#define XGB_LAUNCH(K) K<<<persistentGrid(K, numSMs), kTraceBlock, 0, s>>>
+    if (flat && sc.blasLayout == 1) {
+        if (count) XGB_LAUNCH((k_trace_wide<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else XGB_LAUNCH((k_trace_wide<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    } else if (flat && sc.blasLayout == 0) {
+        if (count) XGB_LAUNCH((k_trace_flat2<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else XGB_LAUNCH((k_trace_flat2<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    } else if (count) {
+        XGB_LAUNCH((k_extend<true>))(sc, q, h, ctrl);
+    } else {
+        XGB_LAUNCH((k_extend<false>))(sc, q, h, ctrl);
     }
-    if (count) k_extend<true><<<grid, kTraceBlock, 0, s>>>(sc, q, h, ctrl);
-    else k_extend<false><<<grid, kTraceBlock, 0, s>>>(sc, q, h, ctrl);
 }
-void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int grid,
+void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s) {
-    if (sc.nInstances <= kFlatInstances) {
-        k_trace_flat<true, false><<<grid, kTraceBlock, 0, s>>>(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
-        return;
-    }
-    k_shadow<<<grid, kTraceBlock, 0, s>>>(sc, rp, sq, out, ctrl);
+    const bool flat = sc.nInstances <= kFlatInstances;
+    if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else if (flat && sc.blasLayout == 0) XGB_LAUNCH((k_trace_flat2<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else XGB_LAUNCH(k_shadow)(sc, rp, sq, out, ctrl);
+#undef XGB_LAUNCH
 }
 
 }  // namespace xgb

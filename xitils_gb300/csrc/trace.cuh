@@ -16,7 +16,7 @@
 
 namespace xgb {
 
-constexpr int kStackDepth = 64;
+constexpr int kStackDepth = 64;  // binary top-level traversal
 // Upper bound on loop iterations of one traversal; a well-formed BVH never
 // comes close. Exceeding it sets error bit 4 and ends the traversal.
 constexpr int kMaxVisits = 1 << 22;
@@ -118,9 +118,104 @@ __device__ __forceinline__ V3 xformVectorRn(const float* m, V3 v) {
               __fadd_rn(__fadd_rn(__fmul_rn(m[8], v.x), __fmul_rn(m[9], v.y)), __fmul_rn(m[10], v.z)));
 }
 
-// Traverses one mesh BVH. ANY: returns at the first accepted hit.
+// ---- 8-wide compressed mesh BVH (WNode, xgb_types.h) ---------------------------
+constexpr int kWideStack = 32;  // (node << 8 | remaining hit mask) entries
+
+struct WideHdr {
+    unsigned int imask;
+    int childBase, triBase;
+    unsigned int meta0, meta1;
+};
+
+__device__ __forceinline__ int rayOctant(const WRay& r) {
+    return (__float_as_uint(r.ix) >> 31) | ((__float_as_uint(r.iy) >> 31) << 1) | ((__float_as_uint(r.iz) >> 31) << 2);
+}
+
+__device__ __forceinline__ unsigned int byteOf(unsigned int w, int s) { return (w >> (8 * (s & 3))) & 0xFFu; }
+
+__device__ __forceinline__ void wideHeader(const WNode* nd, WideHdr& h) {
+    const float4 a = __ldg(&nd->a), b = __ldg(&nd->b);
+    h.imask = __float_as_uint(a.w) >> 24;
+    h.childBase = __float_as_int(b.x);
+    h.triBase = __float_as_int(b.y);
+    h.meta0 = __float_as_uint(b.z);
+    h.meta1 = __float_as_uint(b.w);
+}
+
+// Tests the eight child boxes of a node; returns the hit children as bits at
+// position slot ^ oct (lowest bit first = roughly nearest first).
+// Per axis the plane distance is t = q * (2^e / d) + (p - o) / d, one FMA per
+// plane, with the byte q turned into a float exactly (0x4B0000qq - 2^23). The
+// near plane of each axis is the low one for a positive direction component
+// and the high one for a negative one. The quantised boxes already reach one
+// quantisation step beyond the child's true box, which covers the rounding of
+// this form; the far distance is widened by 2^-20 relative as in slab().
+__device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r, int oct, float tMax, WideHdr& h) {
+    const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c), d = __ldg(&nd->d), e = __ldg(&nd->e);
+    const unsigned int bits = __float_as_uint(a.w);
+    h.imask = bits >> 24;
+    h.childBase = __float_as_int(b.x);
+    h.triBase = __float_as_int(b.y);
+    h.meta0 = __float_as_uint(b.z);
+    h.meta1 = __float_as_uint(b.w);
+    const float scx = __uint_as_float((bits & 0xFFu) << 23) * r.ix;
+    const float scy = __uint_as_float(((bits >> 8) & 0xFFu) << 23) * r.iy;
+    const float scz = __uint_as_float(((bits >> 16) & 0xFFu) << 23) * r.iz;
+    const float bx = (a.x - r.ox) * r.ix, by = (a.y - r.oy) * r.iy, bz = (a.z - r.oz) * r.iz;
+    const unsigned int lx0 = __float_as_uint(c.x), lx1 = __float_as_uint(c.y);
+    const unsigned int ly0 = __float_as_uint(c.z), ly1 = __float_as_uint(c.w);
+    const unsigned int lz0 = __float_as_uint(d.x), lz1 = __float_as_uint(d.y);
+    const unsigned int hx0 = __float_as_uint(d.z), hx1 = __float_as_uint(d.w);
+    const unsigned int hy0 = __float_as_uint(e.x), hy1 = __float_as_uint(e.y);
+    const unsigned int hz0 = __float_as_uint(e.z), hz1 = __float_as_uint(e.w);
+    const bool fx = oct & 1, fy = oct & 2, fz = oct & 4;
+    const unsigned int nx[2] = {fx ? hx0 : lx0, fx ? hx1 : lx1}, xx[2] = {fx ? lx0 : hx0, fx ? lx1 : hx1};
+    const unsigned int ny[2] = {fy ? hy0 : ly0, fy ? hy1 : ly1}, xy[2] = {fy ? ly0 : hy0, fy ? ly1 : hy1};
+    const unsigned int nz[2] = {fz ? hz0 : lz0, fz ? hz1 : lz1}, xz[2] = {fz ? lz0 : hz0, fz ? lz1 : hz1};
+    unsigned int mask = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int w = s >> 2;
+        const unsigned int sel = 0x7540u | (unsigned int)(s & 3);
+        const unsigned int mb = byteOf(w ? h.meta1 : h.meta0, s);
+        if (!((h.imask >> s) & 1u) && mb == 0u) continue;  // empty slot
+        const float qnx = __uint_as_float(__byte_perm(nx[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float qny = __uint_as_float(__byte_perm(ny[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float qnz = __uint_as_float(__byte_perm(nz[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float qfx = __uint_as_float(__byte_perm(xx[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float qfy = __uint_as_float(__byte_perm(xy[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float qfz = __uint_as_float(__byte_perm(xz[w], 0x4B000000u, sel)) - 8388608.0f;
+        const float tn = fmaxf(fmaxf(fmaf(qnx, scx, bx), fmaf(qny, scy, by)), fmaxf(fmaf(qnz, scz, bz), 0.0f));
+        const float tf = fminf(fminf(fmaf(qfx, scx, bx), fmaf(qfy, scy, by)), fminf(fmaf(qfz, scz, bz), tMax));
+        if (tn <= tf * 1.00000095367431640625f) mask |= 1u << (s ^ oct);
+    }
+    return mask;
+}
+
+// Watertight tests of `cnt` triangles from `first`; ANY: stops at the first hit.
+template <bool ANY>
+__device__ __forceinline__ bool testTris(const TriV* tris, int first, int cnt, const WRay& r, float& tMax, TraceHit& hit,
+                                         int inst) {
+    bool found = false;
+    for (int k = 0; k < cnt; ++k) {
+        const TriV* tv = tris + first + k;
+        const float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
+        float t, b0, b1;
+        if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+            tMax = t;
+            found = true;
+            if (ANY) return true;
+            hit.t = t; hit.b0 = b0; hit.b1 = b1;
+            hit.prim = __float_as_int(p0.w);
+            hit.inst = inst;
+        }
+    }
+    return found;
+}
+
+// Traverses one binary mesh BVH (Node2). ANY: returns at the first accepted hit.
 template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
+__device__ __forceinline__ bool traverseBlas2(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
                                              unsigned int* errors, WorkCount& wc) {
     int stack[kStackDepth];
     int sp = 0;
@@ -130,7 +225,7 @@ __device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, fl
         if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
         if (node >= 0) {
             if (COUNT) wc.nodes++;
-            const Node2* nd = m.nodes + node;
+            const Node2* nd = m.nodes2 + node;
             float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
             int4 d = __ldg(&nd->d);
             float t0, t1;
@@ -171,6 +266,62 @@ __device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, fl
         }
     }
     return found;
+}
+
+// Traverses one 8-wide mesh BVH (WNode). ANY: returns at the first accepted hit.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
+                                                 unsigned int* errors, WorkCount& wc) {
+    if (m.rootIsLeaf) {
+        if (COUNT) wc.tris += m.nTris;
+        return testTris<ANY>(m.tris, 0, m.nTris, r, tMax, hit, inst);
+    }
+    const int oct = rayOctant(r);
+    unsigned int stack[kWideStack];
+    int sp = 0;
+    WideHdr h;
+    int node = 0;
+    unsigned int mask = wideEval(m.nodes, r, oct, tMax, h);
+    if (COUNT) wc.nodes++;
+    bool found = false;
+    for (int guard = 0;; ++guard) {
+        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (mask == 0u) {
+            if (sp == 0) break;
+            const unsigned int e = stack[--sp];
+            node = (int)(e >> 8);
+            mask = e & 0xFFu;
+            wideHeader(m.nodes + node, h);
+            continue;
+        }
+        const int slot = (__ffs(mask) - 1) ^ oct;
+        mask &= mask - 1u;
+        const unsigned int mb = byteOf(slot >> 2 ? h.meta1 : h.meta0, slot);
+        if ((h.imask >> slot) & 1u) {
+            if (mask) {
+                if (sp >= kWideStack) { atomicOr(errors, 1u); return found; }
+                stack[sp++] = ((unsigned int)node << 8) | mask;
+            }
+            node = h.childBase + (int)mb;
+            mask = wideEval(m.nodes + node, r, oct, tMax, h);
+            if (COUNT) wc.nodes++;
+        } else {
+            const int cnt = (int)(mb >> 5);
+            if (COUNT) wc.tris += cnt;
+            if (testTris<ANY>(m.tris, h.triBase + (int)(mb & 31u), cnt, r, tMax, hit, inst)) {
+                found = true;
+                if (ANY) return true;
+            }
+        }
+    }
+    return found;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
+                                             unsigned int* errors, WorkCount& wc) {
+    return m.wide ? traverseBlasWide<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc)
+                  : traverseBlas2<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc);
 }
 
 // Scene::intersect (ANY = false) / Scene::intersectAny (ANY = true).

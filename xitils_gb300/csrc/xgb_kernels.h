@@ -11,22 +11,29 @@ namespace xgb {
 // ---- BVH build (bvh_build.cu) ------------------------------------------------
 constexpr int kBuilderPloc = 0;  // locally-ordered clustering (default)
 constexpr int kBuilderLbvh = 1;  // Morton-split linear BVH
+constexpr int kLayoutBinary = 0;  // Node2, two children per 64-byte node
+constexpr int kLayoutWide = 1;    // WNode, eight quantised children per 80-byte node
 struct BlasBuildInput {
     const float4* pos;  // device, object space
     const int* idx;     // device, 3 per triangle
     int nTris;
     int builder;        // kBuilderPloc or kBuilderLbvh
+    int layout;         // kLayoutBinary or kLayoutWide
 };
 struct BlasBuildOutput {
-    Node2* nodes;       // device, nTris - 1 entries (nTris >= 2)
-    TriV* tris;         // device, nTris entries (leaf order)
+    WNode* nodes;       // wide layout: device, allocated by buildBlas (cudaMalloc, nWide entries; the caller frees it)
+    int nWide;
+    Node2* nodes2;      // binary layout: device, allocated by buildBlas (nTris - 1 entries; the caller frees it)
+    int wide;
+    TriV* tris;         // device, nTris entries (leaf order), allocated by the caller
     float4* gnrm;       // device, nTris entries (original order)
     float* triArea;     // device, nTris entries (original order)
     int rootIsLeaf;
     int rootLeaf;
     float boundsLo[3], boundsHi[3];  // object-space bounds of the vertices used
 };
-// Builds a binary BVH over the triangles on `stream` and synchronises it.
+// Builds a binary BVH over the triangles (PLOC or LBVH), in the binary layout or
+// converted into an 8-wide compressed BVH, on `stream`, and synchronises it.
 // Returns a CUDA error code (cudaSuccess on success).
 cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream_t stream);
 
@@ -121,16 +128,16 @@ struct RenderParams {
 
 void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s);
 void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
-void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int grid, bool count, cudaStream_t s);
+// Extension / shadow rays of the wavefront; persistent grids sized from the
+// launched kernel's occupancy on numSMs SMs.
+void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, bool count, cudaStream_t s);
 void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
                  Ctrl* ctrl, int grid, cudaStream_t s);
-void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int grid,
+void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s);
 // Ray queries on a built scene: rays o (xyz, w = tMax) and d; closest hits as 2 float4
 // per ray (t, bits(instance), bits(triangle), -; b0, b1, -, -) or any-hit flags.
 void launchQuery(const SceneDev& sc, const float4* o, const float4* d, int n, int any, float4* hits, int* occluded,
                  unsigned int* errors, int grid, cudaStream_t s);
-int extendBlocksPerSM();
-int shadowBlocksPerSM();
 
 }  // namespace xgb

@@ -24,7 +24,25 @@ struct __align__(16) Node2 {
 };
 static_assert(sizeof(Node2) == 64, "Node2 size");
 
-constexpr int kLeafMax = 4;  // triangles per BLAS leaf
+constexpr int kLeafMax = 4;  // triangles per leaf of a binary (top-level) BVH
+
+// 8-wide mesh BVH node with 8-bit quantised child boxes (80 bytes, five 16-byte
+// loads), after Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on
+// GPUs Through Compressed Wide BVHs" (HPG 2017), with a layout of our own:
+//   a: origin p.xyz, bits: exponent bytes ex | ey << 8 | ez << 16 | imask << 24
+//      (child box plane = p + q * 2^(e - 127); imask bit s = slot s is an inner node)
+//   b: childBase, triBase, meta[0..3], meta[4..7] (one byte per slot)
+//   c: qlo.x[0..7], qlo.y[0..7];  d: qlo.z[0..7], qhi.x[0..7];  e: qhi.y[0..7], qhi.z[0..7]
+// meta of an inner child: its index among the node's inner children (node
+// childBase + meta); of a leaf child: count << 5 | offset, its 1..3 triangles
+// at triBase + offset; 0 with the imask bit clear: an empty slot. Slots are
+// filled so that for a ray whose direction has sign bits `oct`, visiting slot
+// positions slot ^ oct in increasing order goes roughly front to back.
+struct __align__(16) WNode {
+    float4 a, b, c, d, e;
+};
+static_assert(sizeof(WNode) == 80, "WNode size");
+constexpr int kWideLeafMax = 3;  // triangles per leaf child of a WNode
 
 __host__ __device__ inline int leafEncode(int first, int count) { return ~((first << 4) | (count - 1)); }
 __host__ __device__ inline int leafFirst(int code) { return (~code) >> 4; }
@@ -38,7 +56,9 @@ struct __align__(16) TriV {
 };
 
 struct MeshDev {
-    const Node2* nodes;
+    const Node2* nodes2;  // binary BVH (root at 0) when !wide
+    const WNode* nodes;   // 8-wide BVH (root at 0) when wide
+    int wide;
     const TriV* tris;
     const float4* pos;   // object-space positions (w = 0)
     const float2* uv;    // nullptr when absent
@@ -50,8 +70,8 @@ struct MeshDev {
     const float* triArea;  // TriangleIndexed::surfaceArea per triangle
     int nTris;
     int nVerts;
-    int rootIsLeaf;  // 1 when the whole mesh is a single leaf (nodes unused)
-    int rootLeaf;    // leaf code of that leaf
+    int rootIsLeaf;  // 1 when the whole mesh is one leaf (no nodes): <= kLeafMax triangles (binary), <= kWideLeafMax (wide)
+    int rootLeaf;    // leafEncode(0, nTris) of that leaf
 };
 
 struct __align__(16) Instance {
@@ -115,6 +135,7 @@ struct SceneDev {
     const Node2* tlas;
     int nInstances;
     int tlasRootIsLeaf;
+    int blasLayout;  // every mesh binary (0), every mesh wide (1), or a mix (2)
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;
