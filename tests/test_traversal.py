@@ -64,7 +64,7 @@ def test_queries_match_oracle(ctx, builder, layout, make):
           f"t differs {np.sum(hg[:, 0] != hc[:, 0])} (same triangle: {np.sum((hg[:, 0] != hc[:, 0]) & same)})")
     assert same.mean() >= 0.997
     assert np.array_equal(hg[same, 0], hc[same, 0])               # same triangle: same t, bit for bit
-    np.testing.assert_allclose(hg[hit, 0], hc[hit, 0], rtol=1e-5)
+    np.testing.assert_allclose(hg[hit, 0], hc[hit, 0], rtol=1e-5, atol=1e-6)
     b0, b1 = hg[hit, 3], hg[hit, 4]
     assert np.all((b0 >= 0) & (b1 >= 0) & (b0 + b1 <= 1.0 + 1e-6))
     og, oc = gpu.scene.occluded(rays), cpu.occluded(rays)

@@ -31,6 +31,21 @@ __device__ __forceinline__ void creditPath(const RenderParams& rp, unsigned int 
 
 constexpr int kTraceBlock = 128;
 
+// World-space ray for the instance-box tests of the flat kernels: origin and
+// 1/d only (no watertight constants), computed once per ray.
+struct BoxRay {
+    float ox, oy, oz, ix, iy, iz;
+};
+__device__ __forceinline__ bool instBoxHit(const BoxRay& b, const float4* boxes, int inst, float tMax) {
+    const float4 lo = __ldg(&boxes[2 * inst]), hi = __ldg(&boxes[2 * inst + 1]);
+    float tx0 = (lo.x - b.ox) * b.ix, tx1 = (hi.x - b.ox) * b.ix;
+    float ty0 = (lo.y - b.oy) * b.iy, ty1 = (hi.y - b.oy) * b.iy;
+    float tz0 = (lo.z - b.oz) * b.iz, tz1 = (hi.z - b.oz) * b.iz;
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tMax));
+    return tn <= tf * 1.00000095367431640625f;
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock) k_extend(SceneDev sc, PathQueue q, HitQueue h, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
@@ -121,6 +136,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
     int inst = nInst;  // instance being traversed
     unsigned int ray = 0;
     V3 wo(0.f, 0.f, 0.f), wd(0.f, 0.f, 1.f);
+    BoxRay br{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     WRay r;
     int oct = 0;
     const WNode* nodes = nullptr;
@@ -156,6 +172,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
             else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
             wo = V3(o4.x, o4.y, o4.z);
             wd = V3(d4.x, d4.y, d4.z);
+            br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
             hit.prim = -1;
             hit.inst = -1;
             hit.t = tMax;
@@ -168,13 +185,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
         }
         if (!inMesh) {
             // next instance whose world box the ray still reaches, or the end of the ray
-            WRay wr = makeWRay(wo, wd);
             if (!(ANY && occluded))
-                for (++inst; inst < nInst; ++inst) {
-                    float4 lo = __ldg(&sc.instBox[2 * inst]), hi = __ldg(&sc.instBox[2 * inst + 1]);
-                    float tn;
-                    if (slab(wr, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tMax, tn)) break;
-                }
+                for (++inst; inst < nInst; ++inst)
+                    if (instBoxHit(br, sc.instBox, inst, tMax)) break;
             if ((ANY && occluded) || inst >= nInst) {
                 if (ANY) {
                     if (!occluded) {
@@ -194,7 +207,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
                 const MeshDev& m = sc.meshes[in.mesh];
                 nodes = m.nodes;
                 tris = m.tris;
-                if (in.identity) r = wr;
+                if (in.identity) r = makeWRay(wo, wd);
                 else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
                 if (m.rootIsLeaf) {  // the whole mesh is one leaf: test it below, then the next instance
                     leafFirst = 0;
@@ -305,6 +318,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
     int inst = nInst;  // instance being traversed; nInst = ray finished
     unsigned int ray = 0;
     V3 wo(0.f, 0.f, 0.f), wd(0.f, 0.f, 1.f);
+    BoxRay br{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     WRay r;
     const Node2* nodes = nullptr;
     const TriV* tris = nullptr;
@@ -332,6 +346,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
             else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
             wo = V3(o4.x, o4.y, o4.z);
             wd = V3(d4.x, d4.y, d4.z);
+            br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
             hit.prim = -1;
             hit.inst = -1;
             hit.t = tMax;
@@ -344,12 +359,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
         }
         if (nodeAddr == kSentinel && leafAddr >= 0) {
             // next instance whose world box the ray still reaches
-            WRay wr = makeWRay(wo, wd);
-            for (++inst; inst < nInst; ++inst) {
-                float4 lo = __ldg(&sc.instBox[2 * inst]), hi = __ldg(&sc.instBox[2 * inst + 1]);
-                float tn;
-                if (slab(wr, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tMax, tn)) break;
-            }
+            for (++inst; inst < nInst; ++inst)
+                if (instBoxHit(br, sc.instBox, inst, tMax)) break;
             if (ANY && occluded) inst = nInst;
             if (inst >= nInst) {  // ray finished
                 if (ANY) {
@@ -371,7 +382,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
             const MeshDev& m = sc.meshes[in.mesh];
             nodes = m.nodes2;
             tris = m.tris;
-            if (in.identity) r = wr;
+            if (in.identity) r = makeWRay(wo, wd);
             else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
             sp = 0;
             if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
@@ -443,6 +454,144 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
         atomicAdd(ANY ? &ctrl->shadowRays : &ctrl->extensionRays, (unsigned long long)n);
 }
 
+// ---- single-mesh scenes ------------------------------------------------------
+// When the scene is one instance, traversal runs as a persistent per-lane state
+// machine in the style of Aila & Laine ("Understanding the Efficiency of Ray
+// Traversal on GPUs", HPG 2009): a lane whose ray is finished fetches the next
+// one at once (one atomicAdd per group of lanes), inner nodes and leaves are
+// processed in separate inner loops, and the first leaf a lane reaches is
+// postponed until every lane of the warp holds one, so that the warp tests
+// triangles together. Results are identical to traceScene: the same slab and
+// watertight tests, the same closest-hit acceptance.
+
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
+                                                              ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+    const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
+    unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
+    const Instance& in = sc.instances[0];
+    const MeshDev m = sc.meshes[in.mesh];
+    const bool identity = in.identity != 0;
+    const int lane = threadIdx.x & 31;
+    const unsigned int ltMask = (1u << lane) - 1u;
+    int stack[kStackDepth];
+    int sp = 0;
+    int nodeAddr = kSentinel, leafAddr = 0;
+    unsigned int ray = 0;
+    WRay r;
+    float tMax = 0.0f;
+    TraceHit hit;
+    hit.prim = -1;
+    hit.t = 0.0f;
+    hit.b0 = hit.b1 = 0.0f;
+    bool occluded = false;
+    WorkCount wc;
+    for (int guard = 0;; ++guard) {
+        if (nodeAddr == kSentinel) {
+            // lanes without a ray fetch the next ones together
+            const unsigned int act = __activemask();
+            const int leader = __ffs(act) - 1;
+            unsigned int base = 0;
+            if (lane == leader) base = atomicAdd(head, (unsigned int)__popc(act));
+            base = __shfl_sync(act, base, leader);
+            ray = base + __popc(act & ltMask);
+            if (ray >= n) break;
+            float4 o4, d4;
+            if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
+            else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
+            V3 o(o4.x, o4.y, o4.z), d(d4.x, d4.y, d4.z);
+            if (!identity) {
+                o = xformPointRn(in.matInv, o);
+                d = xformVectorRn(in.matInv, d);
+            }
+            r = makeWRay(o, d);
+            hit.prim = -1;
+            hit.t = tMax;
+            occluded = false;
+            sp = 0;
+            guard = 0;
+            if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
+            else { leafAddr = 0; nodeAddr = 0; }
+        }
+        if (guard > kMaxVisits) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
+        bool searching = true;
+        while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
+            if (COUNT) wc.nodes++;
+            const Node2* nd = m.nodes2 + nodeAddr;
+            float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
+            int4 dd = __ldg(&nd->d);
+            float t0, t1;
+            bool h0 = slab(r, a.x, a.y, a.z, a.w, b.x, b.y, tMax, t0);
+            bool h1 = slab(r, b.z, b.w, c.x, c.y, c.z, c.w, tMax, t1);
+            if (h0 && h1) {
+                int near = dd.x, far = dd.y;
+                if (t1 < t0) { near = dd.y; far = dd.x; }
+                if (sp >= kStackDepth) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
+                stack[sp++] = far;
+                nodeAddr = near;
+            } else if (h0) {
+                nodeAddr = dd.x;
+            } else if (h1) {
+                nodeAddr = dd.y;
+            } else {
+                nodeAddr = sp > 0 ? stack[--sp] : kSentinel;
+            }
+            if (nodeAddr < 0 && leafAddr >= 0) {  // first leaf: postpone it, keep descending
+                searching = false;
+                leafAddr = nodeAddr;
+                nodeAddr = sp > 0 ? stack[--sp] : kSentinel;
+            }
+            if (!__any_sync(__activemask(), searching)) break;
+        }
+        while (leafAddr < 0) {
+            int first = leafFirst(leafAddr), cnt = leafCount(leafAddr);
+            if (COUNT) wc.tris += cnt;
+            for (int k = 0; k < cnt; ++k) {
+                const TriV* tv = m.tris + first + k;
+                float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
+                float t, b0, b1;
+                if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+                    tMax = t;
+                    if (ANY) { occluded = true; break; }
+                    hit.t = t; hit.b0 = b0; hit.b1 = b1;
+                    hit.prim = __float_as_int(p0.w);
+                }
+            }
+            if (ANY && occluded) { leafAddr = 0; nodeAddr = kSentinel; break; }
+            leafAddr = nodeAddr;  // another leaf was postponed: take it next
+            if (nodeAddr < 0) nodeAddr = sp > 0 ? stack[--sp] : kSentinel;
+        }
+        if (nodeAddr == kSentinel && leafAddr >= 0) {  // ray finished
+            if (ANY) {
+                if (!occluded) {
+                    float4 cc = s.c[ray];
+                    filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
+                    int target = __float_as_int(cc.w);
+                    if (target >= 0) out.rng[target] = s.rng[ray];
+                    if (rp.train) creditPath(rp, s.pid[ray], cc);
+                }
+            } else {
+                h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
+                h.inst[ray] = hit.prim >= 0 ? 0 : -1;
+            }
+        }
+    }
+    if (COUNT) {
+        __syncwarp();  // every lane of the warp has left the loop
+        unsigned long long nv = wc.nodes, nt = wc.tris;
+        for (int off = 16; off > 0; off >>= 1) {
+            nv += __shfl_down_sync(0xFFFFFFFFu, nv, off);
+            nt += __shfl_down_sync(0xFFFFFFFFu, nt, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&ctrl->nodeVisits, nv);
+            atomicAdd(&ctrl->triTests, nt);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(ANY ? &ctrl->shadowRays : &ctrl->extensionRays, (unsigned long long)n);
+}
+
 // ---- ray queries (xgb_scene_intersect / xgb_scene_occluded) -------------------
 __global__ void __launch_bounds__(kTraceBlock) k_query(SceneDev sc, const float4* o, const float4* d, int n, int any,
                                                        float4* hits, int* occluded, unsigned int* errors) {
@@ -489,6 +638,9 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
     if (flat && sc.blasLayout == 1) {
         if (count) XGB_LAUNCH((k_trace_wide<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_wide<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    } else if (sc.nInstances == 1 && sc.blasLayout == 0) {
+        if (count) XGB_LAUNCH((k_trace_single<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else XGB_LAUNCH((k_trace_single<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (flat && sc.blasLayout == 0) {
         if (count) XGB_LAUNCH((k_trace_flat2<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_flat2<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
@@ -502,6 +654,8 @@ void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, Pa
                   cudaStream_t s) {
     const bool flat = sc.nInstances <= kFlatInstances;
     if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else if (sc.nInstances == 1 && sc.blasLayout == 0)
+        XGB_LAUNCH((k_trace_single<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (flat && sc.blasLayout == 0) XGB_LAUNCH((k_trace_flat2<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else XGB_LAUNCH(k_shadow)(sc, rp, sq, out, ctrl);
 #undef XGB_LAUNCH

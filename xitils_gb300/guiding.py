@@ -7,6 +7,10 @@ budget T. The guided run trains the network online during the first
 pass of both runs is kept (guided passes are unbiased at any network state,
 because the BSDF remains a sampling strategy of the one-sample MIS). The score
 is relMSE = mean((I - R)^2 / (R^2 + 1e-2)) against the reference.
+
+The reference is finite too: it is rendered as two independent halves A and B,
+and relMSE(A, B) / 4 estimates its own relMSE, which adds to both arms' scores;
+the result reports the raw ratio and the ratio with that estimate taken off.
 """
 from __future__ import annotations
 
@@ -39,6 +43,8 @@ def render_reference(ctx: api.Context, builder: api.GpuSceneBuilder, desc: Scene
 
 
 def _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass=None, sample_base=0):
+    """Progressive passes until time_s has passed; on_pass(elapsed) may return
+    the sample count of the next pass (else pass_spp)."""
     rt = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
     spp = 0
     ctx.synchronize()
@@ -47,10 +53,9 @@ def _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass=None, sa
         elapsed = time.perf_counter() - t0
         if elapsed >= time_s:
             break
-        if on_pass:
-            on_pass(elapsed)
-        rt.render(builder.scene, pass_spp, params, sample_base + spp)
-        spp += pass_spp
+        n = (on_pass(elapsed) if on_pass else None) or pass_spp
+        rt.render(builder.scene, n, params, sample_base + spp)
+        spp += n
     img = rt.download() / max(spp, 1)
     return img, spp, time.perf_counter() - t0
 
@@ -62,15 +67,28 @@ def _warm_up(ctx, builder, desc, params, pass_spp):
     rt.download()
 
 
+def reference_halves(ctx: api.Context, builder, desc: SceneDesc, spp: int, chunk: int = 64):
+    """Plain-path reference as two independent halves: (mean, estimated relMSE of the mean)."""
+    a = render_reference(ctx, builder, desc, spp // 2, chunk=chunk, seed_offset=1 << 20)
+    b = render_reference(ctx, builder, desc, spp // 2, chunk=chunk, seed_offset=(1 << 20) + (1 << 24))
+    ref = 0.5 * (a + b)
+    noise = float(np.mean((a - b) ** 2 / (ref ** 2 + 1e-2))) / 4.0
+    return ref, noise
+
+
 def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0, train_fraction: float = 0.25,
                           reference_spp: int = 16384, pass_spp: int = 1, bsdf_fraction: float = 0.5,
                           lr: float = 1e-3, reference: Optional[np.ndarray] = None, seed: int = 0,
-                          batch_rows: int = 8192, builder=None) -> dict:
+                          batch_rows: int = 8192, builder=None, train_pass_spp: int = 1,
+                          reference_noise: Optional[float] = None) -> dict:
     """Both arms are warmed up by one untimed pass; the guided arm's clock
-    includes its network inference and every training step."""
+    includes its network inference and every training step. Training passes
+    take train_pass_spp samples (one network update per pass), the rest pass_spp."""
     builder = builder if builder is not None else api.load_scene(ctx, desc)
     params = desc.params
-    ref = reference if reference is not None else render_reference(ctx, builder, desc, reference_spp)
+    if reference is None:
+        reference, reference_noise = reference_halves(ctx, builder, desc, reference_spp)
+    ref = reference
     builder.scene.setGuide(None)
     _warm_up(ctx, builder, desc, params, pass_spp)
     plain, plain_spp, plain_t = _timed_passes(ctx, builder, desc, time_s, pass_spp, params)
@@ -86,13 +104,19 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
         if state["training"] and elapsed >= train_fraction * time_s:
             builder.scene.setGuide(guide, bsdf_fraction, train=False)
             state["training"] = False
+        return train_pass_spp if state["training"] else pass_spp
 
     guided, guided_spp, guided_t = _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass)
     builder.scene.setGuide(None)
     rp, rg = relmse(plain, ref), relmse(guided, ref)
+    corrected = None
+    if reference_noise is not None and rg - reference_noise > 0:
+        corrected = (rp - reference_noise) / (rg - reference_noise)
     return {
         "time_s": time_s, "train_fraction": train_fraction, "bsdf_fraction": bsdf_fraction,
-        "reference_spp": reference_spp if reference is None else None,
+        "pass_spp": pass_spp, "train_pass_spp": train_pass_spp, "learning_rate": lr, "batch_rows": batch_rows,
+        "reference_relmse_estimate": reference_noise,
+        "relmse_ratio_reference_noise_removed": corrected,
         "plain": {"spp": plain_spp, "seconds": plain_t, "relmse": rp, "mse": float(np.mean((plain - ref) ** 2))},
         "guided": {"spp": guided_spp, "seconds": guided_t, "relmse": rg, "mse": float(np.mean((guided - ref) ** 2)),
                    "train_steps": guide.steps()},
