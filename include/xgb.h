@@ -216,6 +216,36 @@ typedef struct {
     uint64_t guide_train_steps; /* Adam steps of the learned proposal taken by the call */
 } xgb_render_stats;
 
+/* ------------------------------------------------------- batched renders */
+/* No counterpart in the reference (which renders one RenderTarget at a time):
+ * many render jobs -- each a built scene, its own film, integrator parameters and
+ * sample range -- advanced by one wavefront, so small films keep the GPU busy
+ * next to large ones. Every job's film receives what xgb_render(scene, params,
+ * film, spp_begin, spp_count) would add (same per-path random streams; sums in
+ * another order). At most 255 jobs, films below 2^24 pixels, all scenes of one
+ * context; learned-proposal guiding and AOV planes are not applied here. */
+typedef struct {
+    xgb_scene* scene;
+    xgb_film* film;
+    xgb_integrator_params params;
+    uint32_t spp_begin;
+    uint32_t spp_count;
+} xgb_batch_job;
+typedef struct {
+    int queue_capacity;       /* camera paths in flight; 0 = autotuned */
+    int iterations_per_sync;  /* wavefront iterations between host checks (even); 0 = autotuned */
+    int use_graph;            /* 1: the iterations between checks replay as one CUDA graph */
+} xgb_batch_options;
+/* options = NULL: autotuned values (cached per batch shape: scenes, film sizes,
+ * sample counts; the first call of a new shape runs the autotuner) with graphs. */
+xgb_status xgb_render_batch(const xgb_batch_job* jobs, int n, const xgb_batch_options* options, void* stream);
+/* Times short trial renders (1 sample per pixel of every job, into scratch films)
+ * for queue capacities 2^18 .. 2^21 and 4 / 8 / 16 iterations per check; writes
+ * the fastest to *out and caches it for this batch shape. */
+xgb_status xgb_batch_autotune(const xgb_batch_job* jobs, int n, void* stream, xgb_batch_options* out);
+/* Counters of the last xgb_render_batch of this context. */
+xgb_status xgb_batch_stats_get(xgb_ctx* ctx, xgb_render_stats* out);
+
 /* Counters of the last xgb_render on this scene. Synchronises the stream. */
 xgb_status xgb_render_stats_get(xgb_scene* scene, xgb_render_stats* out, void* stream);
 

@@ -37,6 +37,15 @@ class IntegratorParamsC(C.Structure):
                 ("seed", C.c_uint32), ("queue_capacity", C.c_int)]
 
 
+class BatchJobC(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("film", C.c_void_p), ("params", IntegratorParamsC), ("spp_begin", C.c_uint32),
+                ("spp_count", C.c_uint32)]
+
+
+class BatchOptionsC(C.Structure):
+    _fields_ = [("queue_capacity", C.c_int), ("iterations_per_sync", C.c_int), ("use_graph", C.c_int)]
+
+
 class RenderStatsC(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("iterations", C.c_uint64), ("kernel_launches", C.c_uint64), ("node_visits", C.c_uint64),
@@ -104,6 +113,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_film_device_pointer": [P, C.POINTER(P), C.POINTER(C.c_int)],
         "xgb_render": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
         "xgb_render_stats_get": [P, C.POINTER(RenderStatsC), P],
+        "xgb_render_batch": [C.POINTER(BatchJobC), C.c_int, C.POINTER(BatchOptionsC), P],
+        "xgb_batch_autotune": [C.POINTER(BatchJobC), C.c_int, P, C.POINTER(BatchOptionsC)],
+        "xgb_batch_stats_get": [P, C.POINTER(RenderStatsC)],
         "xgb_scene_set_profiling": [P, C.c_int],
         "xgb_render_noalloc": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
         "xgb_guide_create": [P, C.c_uint32, C.POINTER(P)],
@@ -435,6 +447,43 @@ class RenderTarget:
         f = C.c_int()
         self.ctx.check(self.ctx.lib.xgb_film_device_pointer(self.h, C.byref(p), C.byref(f)), "device_pointer")
         return p.value, bool(f.value)
+
+
+def _batch_jobs(jobs):
+    arr = (BatchJobC * len(jobs))()
+    for k, (scene, target, params, spp_begin, spp_count) in enumerate(jobs):
+        p = params or IntegratorParams()
+        arr[k].scene = scene.h.value
+        arr[k].film = target.h.value
+        arr[k].params = IntegratorParamsC(p.integrator, p.max_depth, p.rr_start, p.rr_prob, p.seed,
+                                          getattr(p, "queue_capacity", 0))
+        arr[k].spp_begin = spp_begin
+        arr[k].spp_count = spp_count
+    return arr
+
+
+def render_batch(ctx: Context, jobs, queue_capacity: int = 0, iterations_per_sync: int = 0, use_graph: bool = True,
+                 stream=None) -> None:
+    """xgb_render_batch: jobs = [(Scene, RenderTarget, IntegratorParams, spp_begin, spp_count), ...];
+    zero options are autotuned (cached per batch shape)."""
+    arr = _batch_jobs(jobs)
+    opt = BatchOptionsC(queue_capacity, iterations_per_sync, int(use_graph))
+    ctx.check(ctx.lib.xgb_render_batch(arr, len(jobs), C.byref(opt), stream), "render_batch")
+
+
+def batch_autotune(ctx: Context, jobs, stream=None) -> dict:
+    arr = _batch_jobs(jobs)
+    out = BatchOptionsC()
+    ctx.check(ctx.lib.xgb_batch_autotune(arr, len(jobs), stream, C.byref(out)), "batch_autotune")
+    return {"queue_capacity": out.queue_capacity, "iterations_per_sync": out.iterations_per_sync,
+            "use_graph": bool(out.use_graph)}
+
+
+def batch_stats(ctx: Context) -> dict:
+    s = RenderStatsC()
+    ctx.check(ctx.lib.xgb_batch_stats_get(ctx.h, C.byref(s)), "batch_stats")
+    return {k: (list(getattr(s, k)) if k in ("kernel_ms", "stage_launches") else int(getattr(s, k)))
+            for k, _ in RenderStatsC._fields_}
 
 
 def write_png(path: str, rgb: np.ndarray) -> None:

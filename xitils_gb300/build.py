@@ -28,7 +28,7 @@ UNITS = {
     "trace.cu": [],
     "integrator.cu": ["-fmad=false"],
     "noalloc.cu": [],
-    "guide.cu": [], "image.cu": [],
+    "guide.cu": [], "image.cu": [], "batch.cu": [],
 }
 
 

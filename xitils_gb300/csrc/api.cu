@@ -212,6 +212,10 @@ static xgb_status cudaFail(xgb_ctx* ctx, cudaError_t e, const char* what) {
 
 static cudaStream_t pick(xgb_ctx* ctx, void* s) { return s ? (cudaStream_t)s : ctx->stream; }
 
+namespace xgb {
+void batchRelease(xgb_ctx* ctx);  // batch.cu: the context's batch queues, arrays and graph
+}
+
 extern "C" {
 
 const char* xgb_version(void) { return "xgb 0.1 sm_103a"; }
@@ -240,6 +244,7 @@ xgb_status xgb_ctx_destroy(xgb_ctx* ctx) {
     if (!ctx) return XGB_INVALID_ARG;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    batchRelease(ctx);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return XGB_OK;
@@ -1238,6 +1243,8 @@ bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp
     *fp64 = f->fp64;
     return true;
 }
+xgb_ctx* sceneContext(xgb_scene* s) { return s ? s->ctx : nullptr; }
+xgb_status contextFail(xgb_ctx* ctx, xgb_status st, const std::string& msg) { return fail(ctx, st, msg); }
 bool filmPlane(xgb_film* f, void** d, int* w, int* h, int* fp64, int* device, cudaStream_t* ctxStream) {
     if (!f) return false;
     *d = f->d;

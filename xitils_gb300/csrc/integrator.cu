@@ -46,6 +46,46 @@ __device__ __forceinline__ void aovAdd(const RenderParams& rp, int pix, V3 albed
     }
 }
 
+// Job policies: which scene and render parameters a path belongs to.
+// One scene (xgb_render): the queue's pixel field is the pixel index itself.
+struct OneJob {
+    SceneDev sc;
+    RenderParams rp;
+    __device__ __forceinline__ int locate(unsigned long long g, unsigned long long& local) const {
+        local = g;
+        return 0;
+    }
+    __device__ __forceinline__ const SceneDev& scene(int) const { return sc; }
+    __device__ __forceinline__ const RenderParams& params(int) const { return rp; }
+    __device__ __forceinline__ void decode(int packed, int& job, int& pix) const { job = 0; pix = packed; }
+    __device__ __forceinline__ int encode(int, int pix) const { return pix; }
+};
+// Many scenes in one wavefront (xgb_render_batch): job j owns the global path
+// ids [start[j], start[j+1]); the pixel field carries job << 24 | pixel.
+struct ManyJobs {
+    const SceneDev* sc;
+    const RenderParams* rp;
+    const unsigned long long* start;  // nJobs + 1 prefix sums of W * H * spp
+    int nJobs;
+    __device__ __forceinline__ int locate(unsigned long long g, unsigned long long& local) const {
+        int lo = 0, hi = nJobs - 1;
+        while (lo < hi) {  // last job whose start is <= g
+            const int mid = (lo + hi + 1) >> 1;
+            if (start[mid] <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        local = g - start[lo];
+        return lo;
+    }
+    __device__ __forceinline__ const SceneDev& scene(int j) const { return sc[j]; }
+    __device__ __forceinline__ const RenderParams& params(int j) const { return rp[j]; }
+    __device__ __forceinline__ void decode(int packed, int& job, int& pix) const {
+        job = (int)((unsigned int)packed >> 24);
+        pix = packed & 0xFFFFFF;
+    }
+    __device__ __forceinline__ int encode(int job, int pix) const { return (job << 24) | pix; }
+};
+
 __global__ void k_plan(Ctrl* c, unsigned int capacity) {
     unsigned int nCont = c->nOut;
     unsigned long long remain = c->totalPaths - c->nextPath;
@@ -64,14 +104,19 @@ __global__ void k_plan(Ctrl* c, unsigned int capacity) {
 
 // Camera paths: RenderTargetTile::GenerateFilmPosition (RenderTarget.h:68-80)
 // then PinholeCamera::generateRay (Camera.h:45-55).
-__global__ void __launch_bounds__(kShadeBlock) k_generate(SceneDev sc, RenderParams rp, PathQueue q, const Ctrl* ctrl) {
+template <class J>
+__global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, const Ctrl* ctrl) {
     const unsigned int nCont = ctrl->nCont, nActive = ctrl->nActive;
     const unsigned long long firstNew = ctrl->firstNew;
-    const unsigned int px = (unsigned int)rp.width * (unsigned int)rp.height;
     for (unsigned int s = nCont + blockIdx.x * blockDim.x + threadIdx.x; s < nActive; s += gridDim.x * blockDim.x) {
-        unsigned long long g = firstNew + (s - nCont);
-        unsigned int sample = rp.sppBegin + (unsigned int)(g / px);
-        unsigned int pix = (unsigned int)(g % px);
+        const unsigned long long g = firstNew + (s - nCont);
+        unsigned long long local;
+        const int job = jobs.locate(g, local);
+        const SceneDev& sc = jobs.scene(job);
+        const RenderParams& rp = jobs.params(job);
+        const unsigned int px = (unsigned int)rp.width * (unsigned int)rp.height;
+        unsigned int sample = rp.sppBegin + (unsigned int)(local / px);
+        unsigned int pix = (unsigned int)(local % px);
         int x = (int)(pix % (unsigned int)rp.width), y = (int)(pix / (unsigned int)rp.width);
         Pcg rng;
         rng.seed(pix, sample, rp.seed);
@@ -87,7 +132,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_generate(SceneDev sc, RenderPar
         int len = rp.integrator == 0 ? 2 : 1;
         q.o[s] = make_float4(o.x, o.y, o.z, 0.0f);
         q.d[s] = make_float4(d.x, d.y, d.z, __int_as_float(len | (FLAG_PRIMARY << 16)));
-        q.thr[s] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float((int)pix));
+        q.thr[s] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(jobs.encode(job, (int)pix)));
         q.rng[s] = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
         if (rp.train) {
             q.grec[s] = -1;
@@ -181,13 +226,13 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
     mx.lobe[4].alpha = a1.x; mx.lobe[5].alpha = a1.y; mx.lobe[6].alpha = a1.z; mx.lobe[7].alpha = a1.w;
 }
 
-__global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams rp, PathQueue in, HitQueue hq,
-                                                       PathQueue out, ShadowQueue sq, Ctrl* ctrl) {
+template <class J>
+__global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
+                                                       ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
     const int lane = threadIdx.x & 31;
     const unsigned int warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned int nWarps = (gridDim.x * blockDim.x) >> 5;
-    const bool naive = rp.integrator == 1;
     for (unsigned int base = warpId * 32u; base < n; base += nWarps * 32u) {
         const unsigned int i = base + lane;
         bool cont = false, shadow = false, done = false;
@@ -203,7 +248,12 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
             const int meta = __float_as_int(d4.w);
             int len = meta & 0xFFFF;
             const int flags = meta >> 16;
-            const int pix = __float_as_int(t4.w);
+            const int packed = __float_as_int(t4.w);
+            int job, pix;
+            jobs.decode(packed, job, pix);
+            const SceneDev& sc = jobs.scene(job);
+            const RenderParams& rp = jobs.params(job);
+            const bool naive = rp.integrator == 1;
             const float pdfPrev = o4.w;
             V3 dir(d4.x, d4.y, d4.z);
             V3 thr(t4.x, t4.y, t4.z);
@@ -258,7 +308,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                         V3 no = s.p + kRayOffset * wi;
                         r.o = make_float4(no.x, no.y, no.z, pdf);
                         r.d = make_float4(wi.x, wi.y, wi.z, __int_as_float(len));
-                        r.thr = make_float4(thr.x, thr.y, thr.z, __int_as_float(pix));
+                        r.thr = make_float4(thr.x, thr.y, thr.z, __int_as_float(packed));
                         r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
                         cont = true;
                     } else {
@@ -354,7 +404,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                                     V3 Le = emission(sc.materials[ls.material], -sd, ls.n);
                                     V3 c = thr * mis * bc * Le * G / ls.pdf;
                                     r.so = make_float4(so.x, so.y, so.z, stMax);
-                                    r.sd = make_float4(sd.x, sd.y, sd.z, __int_as_float(pix));
+                                    r.sd = make_float4(sd.x, sd.y, sd.z, __int_as_float(packed));
                                     r.sc = make_float4(c.x, c.y, c.z, 0.0f);
                                     r.stochastic = spec.state != rng.state;
                                     r.srng = make_uint2((unsigned int)spec.state, (unsigned int)(spec.state >> 32));
@@ -367,7 +417,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
                             V3 no = s.p + kRayOffset * wi;
                             r.o = make_float4(no.x, no.y, no.z, pdf);
                             r.d = make_float4(wi.x, wi.y, wi.z, __int_as_float(len + 1));
-                            r.thr = make_float4(thrNext.x, thrNext.y, thrNext.z, __int_as_float(pix));
+                            r.thr = make_float4(thrNext.x, thrNext.y, thrNext.z, __int_as_float(packed));
                             r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
                             cont = true;
                             if (rp.train && guidedHere && pdf > 0.0f && keepRecord(pid, len, rp.recordProb)) {
@@ -407,12 +457,13 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
         if (lane == 0 && mc) oc = atomicAdd(&ctrl->nOut, (unsigned int)__popc(mc));
         oc = __shfl_sync(kFull, oc, 0);
         unsigned int slot = oc + __popc(mc & ((1u << lane) - 1u));
+        const bool train = jobs.params(0).train;  // guide training runs with one job only
         if (cont) {
             out.o[slot] = r.o;
             out.d[slot] = r.d;
             out.thr[slot] = r.thr;
             out.rng[slot] = r.rng;
-            if (rp.train) {
+            if (train) {
                 out.grec[slot] = r.grec;
                 out.pid[slot] = in.pid[i];
             }
@@ -428,7 +479,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
             r.sc.w = __int_as_float((r.stochastic && cont) ? (int)slot : -1);
             sq.c[ss] = r.sc;
             sq.rng[ss] = r.srng;
-            if (rp.train) sq.pid[ss] = in.pid[i];
+            if (train) sq.pid[ss] = in.pid[i];
         }
         unsigned int md = __ballot_sync(kFull, done);
         if (lane == 0 && md) atomicAdd(&ctrl->pathsDone, (unsigned long long)__popc(md));
@@ -438,12 +489,21 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(SceneDev sc, RenderParams
 void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s) { k_plan<<<1, 1, 0, s>>>(ctrl, capacity); }
 
 void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s) {
-    k_generate<<<grid, kShadeBlock, 0, s>>>(sc, rp, q, ctrl);
+    k_generate<OneJob><<<grid, kShadeBlock, 0, s>>>(OneJob{sc, rp}, q, ctrl);
 }
 
 void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
                  Ctrl* ctrl, int grid, cudaStream_t s) {
-    k_shade<<<grid, kShadeBlock, 0, s>>>(sc, rp, in, h, out, sq, ctrl);
+    k_shade<OneJob><<<grid, kShadeBlock, 0, s>>>(OneJob{sc, rp}, in, h, out, sq, ctrl);
+}
+
+void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s) {
+    k_generate<ManyJobs><<<grid, kShadeBlock, 0, s>>>(ManyJobs{b.scenes, b.params, b.start, b.nJobs}, q, ctrl);
+}
+
+void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+                      cudaStream_t s) {
+    k_shade<ManyJobs><<<grid, kShadeBlock, 0, s>>>(ManyJobs{b.scenes, b.params, b.start, b.nJobs}, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb

@@ -592,6 +592,58 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_single(SceneDev sc, Rende
         atomicAdd(ANY ? &ctrl->shadowRays : &ctrl->extensionRays, (unsigned long long)n);
 }
 
+// ---- batches of scenes (xgb_render_batch) -----------------------------------------
+// Each ray finds its job (and so its scene) in the high bits of its pixel field
+// and is traced by the general two-level traversal.
+__global__ void __launch_bounds__(kTraceBlock) k_extend_batch(BatchView b, PathQueue q, HitQueue h, Ctrl* ctrl) {
+    const unsigned int n = ctrl->nActive;
+    const int lane = threadIdx.x & 31;
+    WorkCount wc;
+    for (;;) {
+        unsigned int base = 0;
+        if (lane == 0) base = atomicAdd(&ctrl->extendHead, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const unsigned int i = base + lane;
+        if (i < n) {
+            const float4 o = q.o[i], d = q.d[i];
+            const int job = (int)(__float_as_uint(q.thr[i].w) >> 24);
+            TraceHit hit;
+            traceScene<false>(b.scenes[job], V3(o.x, o.y, o.z), V3(d.x, d.y, d.z), __int_as_float(0x7f800000), hit,
+                              &ctrl->errors, wc);
+            h.h[i] = make_float4(hit.t, hit.b0, hit.b1, __int_as_float(hit.prim));
+            h.inst[i] = hit.inst;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctrl->extensionRays, (unsigned long long)n);
+}
+
+__global__ void __launch_bounds__(kTraceBlock) k_shadow_batch(BatchView b, ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+    const unsigned int n = ctrl->nShadow;
+    const int lane = threadIdx.x & 31;
+    WorkCount wc;
+    for (;;) {
+        unsigned int base = 0;
+        if (lane == 0) base = atomicAdd(&ctrl->shadowHead, 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const unsigned int i = base + lane;
+        if (i < n) {
+            const float4 o = s.o[i], d = s.d[i];
+            const unsigned int packed = __float_as_uint(d.w);
+            const int job = (int)(packed >> 24), pix = (int)(packed & 0xFFFFFFu);
+            TraceHit hit;
+            if (!traceScene<true>(b.scenes[job], V3(o.x, o.y, o.z), V3(d.x, d.y, d.z), o.w, hit, &ctrl->errors, wc)) {
+                const float4 c = s.c[i];
+                filmAdd(b.params[job], pix, V3(c.x, c.y, c.z));
+                const int target = __float_as_int(c.w);
+                if (target >= 0) out.rng[target] = s.rng[i];
+            }
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctrl->shadowRays, (unsigned long long)n);
+}
+
 // ---- ray queries (xgb_scene_intersect / xgb_scene_occluded) -------------------
 __global__ void __launch_bounds__(kTraceBlock) k_query(SceneDev sc, const float4* o, const float4* d, int n, int any,
                                                        float4* hits, int* occluded, unsigned int* errors) {
@@ -650,6 +702,13 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
         XGB_LAUNCH((k_extend<false>))(sc, q, h, ctrl);
     }
 }
+void launchExtendBatch(const BatchView& b, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, cudaStream_t s) {
+    XGB_LAUNCH(k_extend_batch)(b, q, h, ctrl);
+}
+void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs, cudaStream_t s) {
+    XGB_LAUNCH(k_shadow_batch)(b, sq, out, ctrl);
+}
+
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s) {
     const bool flat = sc.nInstances <= kFlatInstances;

@@ -126,6 +126,20 @@ struct RenderParams {
     float4* pathAcc;          // per path of the call: contributions so far (rgb)
 };
 
+// Device arrays of a batch of render jobs sharing one wavefront (xgb_render_batch):
+// a path of job j carries j << 24 | pixel in its pixel field.
+struct BatchView {
+    const SceneDev* scenes;
+    const RenderParams* params;
+    const unsigned long long* start;  // nJobs + 1 prefix sums of the jobs' path counts
+    int nJobs;
+};
+void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
+void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+                      cudaStream_t s);
+void launchExtendBatch(const BatchView& b, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, cudaStream_t s);
+void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs, cudaStream_t s);
+
 void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s);
 void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
 // Extension / shadow rays of the wavefront; persistent grids sized from the

@@ -301,3 +301,48 @@ def occluded_room(width: int = 1024, height: int = 1024, spp: int = 4, n_boxes: 
     s.add_object(s.add_mesh(pos, idx), light)
     s.set_camera(look_at((1.2, 2.6, 1.0), (6.0, 1.6, 6.5), (0, 1, 0)), 70.0 * math.pi / 180.0, height / width)
     return s
+
+
+# ------------------------------------------------------------ batched scenes --
+BATCH_RESOLUTIONS = (128, 256, 512, 1024)
+
+
+def batch_scene(index: int, seed: int = 21, tris_range=(1_000, 500_000), resolutions=BATCH_RESOLUTIONS,
+                spp: int = 32, max_depth: int = 8) -> SceneDesc:
+    """One scene of the batched-rendering workload: a seeded random triangle soup
+    or fBm heightfield in the unit box with a triangle count log-uniform in
+    ``tris_range``, split between a Lambert and a GGX (roughness U[0.02, 0.8])
+    material, lit by 1-4 quad lights (radiance U[1, 50]) facing down from above
+    it; square film from ``resolutions``, ``spp`` samples, max depth 8."""
+    rng = np.random.default_rng(seed * 1009 + index)
+    n_tris = int(round(math.exp(rng.uniform(math.log(tris_range[0]), math.log(tris_range[1])))))
+    res = int(rng.choice(resolutions))
+    s = SceneDesc(name=f"batch{index}", width=res, height=res, spp=spp,
+                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=index))
+    lambert = s.diffuse(rng.uniform(0.2, 0.85, 3))
+    ggx = s.metal(float(rng.uniform(0.02, 0.8)), rng.uniform(0.4, 0.95, 3))
+    if rng.uniform() < 0.5:  # triangle soup: two halves, one per material
+        centers = rng.uniform(0.05, 0.95, (n_tris, 3))
+        centers[:, 1] *= 0.6
+        size = 1.6 * n_tris ** (-1.0 / 3.0)
+        offs = rng.normal(scale=size, size=(n_tris, 3, 3))
+        pos = (centers[:, None, :] + offs).reshape(-1, 3).astype(F)
+        half = n_tris // 2
+        for lo, hi, mat in ((0, half, lambert), (half, n_tris, ggx)):
+            if hi > lo:
+                idx = np.arange(3 * lo, 3 * hi, dtype=np.int32) - 3 * lo
+                s.add_object(s.add_mesh(pos[3 * lo:3 * hi], idx), mat)
+    else:  # heightfield: the grid whose triangle count is closest, ground Lambert, a GGX copy raised above it
+        g = max(2, int(round(math.sqrt(n_tris / 2.0))) + 1)
+        heights = fbm_heights(g, int(rng.integers(1 << 30)))
+        hp, huv, hidx = heightfield_mesh(heights)
+        s.add_object(s.add_mesh(hp, hidx, uv=huv), lambert if rng.uniform() < 0.5 else ggx)
+    n_lights = int(rng.integers(1, 5))
+    for k in range(n_lights):
+        cx, cz = rng.uniform(0.2, 0.8, 2)
+        w = float(rng.uniform(0.05, 0.2))
+        y = float(rng.uniform(0.9, 1.3))
+        pos, idx = quad([cx - w, y, cz - w], [cx + w, y, cz - w], [cx + w, y, cz + w], [cx - w, y, cz + w])  # normal -y
+        s.add_object(s.add_mesh(pos, idx), s.emission([float(rng.uniform(1.0, 50.0))] * 3))
+    s.set_camera(look_at((0.5, 1.1, -0.9), (0.5, 0.2, 0.5), (0.0, 1.0, 0.0)), 50.0 * math.pi / 180.0, 1.0)
+    return s
