@@ -61,6 +61,7 @@ struct BatchState {
     unsigned int graphCap = 0;
     int graphIters = 0;
     int graphJobs = 0;
+    int graphFlat = -1;
     std::map<std::string, xgb_batch_options> tuned;
     xgb_render_stats last{};
 };
@@ -168,9 +169,11 @@ std::string shapeKey(const xgb_batch_job* jobs, int n) {
 xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int n, const xgb_batch_options& o,
                     cudaStream_t st, int device, int numSMs, double* seconds) {
     unsigned long long total = 0;
+    int flat = 1;
     for (int i = 0; i < n; ++i) {
         SceneDev sd; int dev, sms, built; cudaStream_t cs;
         sceneView(jobs[i].scene, &sd, &dev, &sms, &cs, &built);
+        if (sd.nInstances > 16 || sd.blasLayout != 0) flat = 0;
         void* fd; int w, h, f64, fdev; cudaStream_t fcs;
         filmPlane(jobs[i].film, &fd, &w, &h, &f64, &fdev, &fcs);
         const xgb_integrator_params& P = jobs[i].params;
@@ -206,13 +209,14 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dStart, b->hStart, sizeof(unsigned long long) * (n + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctrl, b->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return contextFail(ctx, XGB_CUDA_ERROR, std::string("xgb_render_batch: ") + cudaGetErrorString(e));
-    const BatchView v{b->dScenes, b->dParams, b->dStart, n};
+    const BatchView v{b->dScenes, b->dParams, b->dStart, n, flat};
     const int iters = std::max(2, (o.iterations_per_sync + 1) & ~1);
     const auto t0 = std::chrono::steady_clock::now();
     uint64_t launches = 0;
     for (int block = 0;; ++block) {
         const bool replay = o.use_graph && block > 0;  // the first block runs direct (and primes the occupancy cache)
-        if (replay && !(b->graph && b->graphCap == capR && b->graphIters == iters && b->graphJobs == n)) {
+        if (replay && !(b->graph && b->graphCap == capR && b->graphIters == iters && b->graphJobs == n &&
+                        b->graphFlat == flat)) {
             if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
             cudaGraph_t g = nullptr;
             e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
@@ -226,7 +230,7 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
                 b->graph = nullptr;
                 return contextFail(ctx, XGB_CUDA_ERROR, std::string("xgb_render_batch: graph capture: ") + cudaGetErrorString(e));
             }
-            b->graphCap = capR; b->graphIters = iters; b->graphJobs = n;
+            b->graphCap = capR; b->graphIters = iters; b->graphJobs = n; b->graphFlat = flat;
         }
         if (replay) e = cudaGraphLaunch(b->graph, st);
         else { enqueueBlock(b, v, capR, iters, numSMs, st); e = cudaGetLastError(); }

@@ -110,6 +110,24 @@ __global__ void __launch_bounds__(kTraceBlock) k_shadow(SceneDev sc, RenderParam
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctrl->shadowRays, (unsigned long long)n);
 }
 
+// Scene lookup of the flat kernels: one scene (the kernel argument) or one per
+// job of a batch (the job in the high byte of the ray's pixel field).
+struct OneScene {
+    SceneDev sc;
+    RenderParams rp;
+    __device__ __forceinline__ int jobOf(unsigned int) const { return 0; }
+    __device__ __forceinline__ int pixelOf(unsigned int packed) const { return (int)packed; }
+    __device__ __forceinline__ const SceneDev& scene(int) const { return sc; }
+    __device__ __forceinline__ const RenderParams& params(int) const { return rp; }
+};
+struct BatchScenes {
+    BatchView b;
+    __device__ __forceinline__ int jobOf(unsigned int packed) const { return (int)(packed >> 24); }
+    __device__ __forceinline__ int pixelOf(unsigned int packed) const { return (int)(packed & 0xFFFFFFu); }
+    __device__ __forceinline__ const SceneDev& scene(int j) const { return b.scenes[j]; }
+    __device__ __forceinline__ const RenderParams& params(int j) const { return b.params[j]; }
+};
+
 // ---- scenes of a few instances: 8-wide mesh BVHs ------------------------------
 // With at most kFlatInstances instances the top level is a short list: a lane
 // walks the instances in order (those whose world box the ray still reaches
@@ -304,12 +322,13 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
 // same closest-hit acceptance (tMax shrinks across instances).
 constexpr int kSentinel = 0x7FFFFFFF;
 
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
-                                                            ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+template <bool ANY, bool COUNT, class S>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue q, HitQueue h, ShadowQueue s,
+                                                            PathQueue out, Ctrl* ctrl) {
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
     unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
-    const int nInst = sc.nInstances;
+    int job = 0;
+    int nInst = 0;
     const int lane = threadIdx.x & 31;
     const unsigned int ltMask = (1u << lane) - 1u;
     int stack[kStackDepth];
@@ -347,6 +366,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
             wo = V3(o4.x, o4.y, o4.z);
             wd = V3(d4.x, d4.y, d4.z);
             br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
+            job = scenes.jobOf(ANY ? __float_as_uint(d4.w) : __float_as_uint(q.thr[ray].w));
+            nInst = scenes.scene(job).nInstances;
             hit.prim = -1;
             hit.inst = -1;
             hit.t = tMax;
@@ -360,13 +381,14 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
         if (nodeAddr == kSentinel && leafAddr >= 0) {
             // next instance whose world box the ray still reaches
             for (++inst; inst < nInst; ++inst)
-                if (instBoxHit(br, sc.instBox, inst, tMax)) break;
+                if (instBoxHit(br, scenes.scene(job).instBox, inst, tMax)) break;
             if (ANY && occluded) inst = nInst;
             if (inst >= nInst) {  // ray finished
                 if (ANY) {
                     if (!occluded) {
                         float4 cc = s.c[ray];
-                        filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
+                        const RenderParams& rp = scenes.params(job);
+                        filmAdd(rp, scenes.pixelOf(__float_as_uint(s.d[ray].w)), V3(cc.x, cc.y, cc.z));
                         int target = __float_as_int(cc.w);
                         if (target >= 0) out.rng[target] = s.rng[ray];
                         if (rp.train) creditPath(rp, s.pid[ray], cc);
@@ -378,6 +400,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(SceneDev sc, Render
                 fetch = true;
                 continue;
             }
+            const SceneDev& sc = scenes.scene(job);
             const Instance& in = sc.instances[inst];
             const MeshDev& m = sc.meshes[in.mesh];
             nodes = m.nodes2;
@@ -694,8 +717,8 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
         if (count) XGB_LAUNCH((k_trace_single<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_single<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (flat && sc.blasLayout == 0) {
-        if (count) XGB_LAUNCH((k_trace_flat2<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-        else XGB_LAUNCH((k_trace_flat2<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        if (count) XGB_LAUNCH((k_trace_flat2<false, true, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else XGB_LAUNCH((k_trace_flat2<false, false, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (count) {
         XGB_LAUNCH((k_extend<true>))(sc, q, h, ctrl);
     } else {
@@ -703,10 +726,12 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
     }
 }
 void launchExtendBatch(const BatchView& b, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, cudaStream_t s) {
-    XGB_LAUNCH(k_extend_batch)(b, q, h, ctrl);
+    if (b.flat) XGB_LAUNCH((k_trace_flat2<false, false, BatchScenes>))(BatchScenes{b}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    else XGB_LAUNCH(k_extend_batch)(b, q, h, ctrl);
 }
 void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs, cudaStream_t s) {
-    XGB_LAUNCH(k_shadow_batch)(b, sq, out, ctrl);
+    if (b.flat) XGB_LAUNCH((k_trace_flat2<true, false, BatchScenes>))(BatchScenes{b}, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else XGB_LAUNCH(k_shadow_batch)(b, sq, out, ctrl);
 }
 
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
@@ -715,7 +740,8 @@ void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, Pa
     if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (sc.nInstances == 1 && sc.blasLayout == 0)
         XGB_LAUNCH((k_trace_single<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
-    else if (flat && sc.blasLayout == 0) XGB_LAUNCH((k_trace_flat2<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else if (flat && sc.blasLayout == 0)
+        XGB_LAUNCH((k_trace_flat2<true, false, OneScene>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else XGB_LAUNCH(k_shadow)(sc, rp, sq, out, ctrl);
 #undef XGB_LAUNCH
 }

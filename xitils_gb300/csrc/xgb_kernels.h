@@ -133,6 +133,7 @@ struct BatchView {
     const RenderParams* params;
     const unsigned long long* start;  // nJobs + 1 prefix sums of the jobs' path counts
     int nJobs;
+    int flat;  // every scene has <= 16 instances and binary mesh BVHs: the persistent per-lane kernels
 };
 void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
 void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
