@@ -93,6 +93,14 @@ xgb_status xgb_material_diffuse(xgb_ctx* ctx, const float albedo[3], const xgb_t
  * roughness_tex optional: per-hit roughness = red channel of a nearest lookup. */
 xgb_status xgb_material_metal(xgb_ctx* ctx, float roughness, const float f0[3], const xgb_texture* roughness_tex,
                               xgb_material** out);
+/* Opt-in fixes of reference quirks (the reference has none of them; off by
+ * default so that renders match it). XGB_FIX_METAL_HORIZON: Metal reflects
+ * nothing when wo or wi lies below its shading normal and samples nothing for
+ * wo below it (the reference divides by a clamped zero there and returns
+ * inf / NaN, which microfacet normal mapping's random walk over a Metal base
+ * reaches). Applies to materials whose scene is built afterwards. */
+#define XGB_FIX_METAL_HORIZON 1u
+xgb_status xgb_material_set_fixes(xgb_material* material, uint32_t fixes);
 /* Glossy(albedo, sharpness) (Material.h:88-132). */
 xgb_status xgb_material_glossy(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out);
 /* GlossyWithHighLight(albedo, highlight, sharpness, sharpnessHighLight, rate) (Material.h:134-175). */

@@ -193,6 +193,7 @@ int xref_add_material(void* p, int type, const float* f, int base, int tex, int 
         break;
     }
     case ORC_MAT_METAL:
+        if (f[4] != 0.0f) return -1;  // the below-horizon fix is not a reference behaviour
         if (tex >= 0) m = std::make_shared<MetalRoughnessTexture>(s->textures[tex], Vector3f(f[1], f[2], f[3]));
         else m = std::make_shared<Metal>(f[0], Vector3f(f[1], f[2], f[3]));
         break;

@@ -458,6 +458,7 @@ struct Material {
     V3 albedo, f0, highlight, power;
     float roughness = 0, sharpness = 0, sharpnessHL = 0, rate = 0, index = 1;
     int tex = -1, normalmap = -1, base = -1;
+    int fixes = 0;  // bit 0: Metal below-horizon fix
     bool emissive() const { return type == ORC_MAT_EMISSION; }
 };
 
@@ -494,9 +495,14 @@ struct Scene {
 
 // ---- Metal (Material.h:275-384); alpha = roughness^2, roughness from the
 // constant or from a roughness texture (nearest lookup of the red channel).
+// horizon = the below-horizon fix (not the reference's behaviour, which has
+// none): no reflection when wo or wi lies below the shading normal, and no
+// sample for wo below it. Inside microfacet normal mapping's random walk the
+// reference's Metal otherwise divides by a clamped zero and yields NaN.
 struct MetalEval {
     float alpha;
     V3 f0;
+    bool horizon = false;
     V3 F(V3 eye, V3 h) const { return f0 + (V3(1.0f) - f0) * powf(1 - dot(eye, h), 5.0f); }
     float D(V3 x, V3 n) const {
         float alpha2 = alpha * alpha;
@@ -534,6 +540,7 @@ struct MetalEval {
     }
     V3 bsdfCos(const Isect& is, V3 wi) const {
         V3 wo = is.wo, n = is.sn;
+        if (horizon && (dot(wo, n) <= 0.0f || dot(wi, n) <= 0.0f)) return V3(0.0f);
         V3 h = normalize(wi + wo);
         V3 Fr = F(wo, h);
         float Dv = D(h, n);
@@ -542,14 +549,22 @@ struct MetalEval {
     }
     float pdf(const Isect& is, V3 wi) const {
         V3 wo = is.wo, n = is.sn;
+        if (horizon && (dot(wo, n) <= 0.0f || dot(wi, n) <= 0.0f)) return 0.0f;
         V3 h = normalize(wi + wo);
+        if (horizon && !(dot(n, h) > 0.0f && dot(wo, h) > 0.0f)) return 0.0f;
         return DV(h, n, wo) / (4 * dot(wo, h));
     }
     V3 evalAndSample(const Isect& is, Rng& rng, V3* wi, float* pdfOut) const {
         V3 wo = is.wo, n = is.sn;
+        if (horizon && dot(wo, n) <= 0.0f) {
+            *wi = n;
+            *pdfOut = 0.0f;
+            return V3(0.0f);
+        }
         V3 h = sampleVNDF(wo, n, rng);
         *wi = 2 * dot(wo, h) * h - wo;
         *pdfOut = pdf(is, *wi);
+        if (horizon && !(*pdfOut > 0.0f)) return V3(0.0f);
         return bsdfCos(is, *wi) / *pdfOut;
     }
 };
@@ -636,7 +651,7 @@ V3 Shading::bsdfCos(int mi, const Isect& is, Rng& rng, V3 wi) const {
         return m.albedo / M_PI * sc->textures[m.tex].lookup(is.uv) * clampPositive(dot(is.sn, wi));
     case ORC_MAT_METAL: {
         float r = metalRoughness(*sc, m, is);
-        return MetalEval{r * r, m.f0}.bsdfCos(is, wi);
+        return MetalEval{r * r, m.f0, (m.fixes & 1) != 0}.bsdfCos(is, wi);
     }
     case ORC_MAT_GLOSSY: return GlossyEval{m.albedo, m.sharpness, false}.bsdfCos(is, wi);
     case ORC_MAT_GLOSSY_CLAMPED: return GlossyEval{m.albedo, m.sharpness, true}.bsdfCos(is, wi);
@@ -678,7 +693,7 @@ float Shading::getPDF(int mi, const Isect& is, V3 wi) const {
     case ORC_MAT_DIFFUSE: return clampPositive(dot(wi, is.sn)) / M_PI;  // Material.h:78-81
     case ORC_MAT_METAL: {
         float r = metalRoughness(*sc, m, is);
-        return MetalEval{r * r, m.f0}.pdf(is, wi);
+        return MetalEval{r * r, m.f0, (m.fixes & 1) != 0}.pdf(is, wi);
     }
     case ORC_MAT_GLOSSY: return GlossyEval{m.albedo, m.sharpness, false}.pdf(is, wi);
     case ORC_MAT_GLOSSY_CLAMPED: return GlossyEval{m.albedo, m.sharpness, true}.pdf(is, wi);
@@ -727,7 +742,7 @@ V3 Shading::evalAndSample(int mi, const Isect& is, Rng& rng, V3* wi, float* pdf)
     }
     case ORC_MAT_METAL: {
         float r = metalRoughness(*sc, m, is);
-        return MetalEval{r * r, m.f0}.evalAndSample(is, rng, wi, pdf);
+        return MetalEval{r * r, m.f0, (m.fixes & 1) != 0}.evalAndSample(is, rng, wi, pdf);
     }
     case ORC_MAT_GLOSSY: return GlossyEval{m.albedo, m.sharpness, false}.evalAndSample(is, rng, wi, pdf);
     case ORC_MAT_GLOSSY_CLAMPED: return GlossyEval{m.albedo, m.sharpness, true}.evalAndSample(is, rng, wi, pdf);
@@ -1148,7 +1163,7 @@ int xcpu_add_material(void* s, int type, const float* f, int base, int tex, int 
     m.tex = tex; m.normalmap = normalmap; m.base = base;
     switch (type) {
     case ORC_MAT_DIFFUSE: m.albedo = V3(f[0], f[1], f[2]); break;
-    case ORC_MAT_METAL: m.roughness = f[0]; m.f0 = V3(f[1], f[2], f[3]); break;
+    case ORC_MAT_METAL: m.roughness = f[0]; m.f0 = V3(f[1], f[2], f[3]); m.fixes = (int)f[4]; break;
     case ORC_MAT_GLOSSY:
     case ORC_MAT_GLOSSY_CLAMPED: m.albedo = V3(f[0], f[1], f[2]); m.sharpness = f[3]; break;
     case ORC_MAT_GLOSSY_HIGHLIGHT:

@@ -150,3 +150,13 @@ def test_denoiser_aovs(ctx, make, params, color_tol):
     assert relmse(plain, color) <= 1e-9  # enabling the AOV planes leaves the radiance alone
     rt.clear()
     assert not rt.download_aov("albedo").any() and not rt.download_aov("normal").any()
+
+
+def test_mfnm_at_scale_small(ctx):
+    """The normal-mapping-at-scale scene, scaled down: heightfield and boxes under
+    MicrofacetNormalMapping over a textured GGX base, more than 16 instances (the
+    general two-level traversal), environment plus quad lights, depth 12."""
+    desc = scenes.mfnm_at_scale(64, 64, 8, grid=65, n_boxes=20, normal_res=64, env_size=(128, 64))
+    gpu, cpu, err, close = _compare(ctx, desc)
+    assert err <= MFNM_TOL
+    assert abs(gpu.mean() - cpu.mean()) <= 1e-3 * max(cpu.mean(), 1e-3) + 2e-3 * cpu.mean()

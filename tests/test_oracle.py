@@ -133,3 +133,27 @@ def test_oracle_aovs_match_golden(name):
     assert np.array_equal(normal, golden[name + "_normal"])
     plain = load_scene(desc, "port").render_pcg(desc, params=params)
     assert np.array_equal(plain, film)  # the AOVs draw nothing from the paths' streams
+
+
+@needs_ref
+def test_metal_under_normal_mapping_nan_and_the_horizon_fix():
+    """The reference's Metal divides by a clamped zero for wo below its shading
+    normal, which microfacet normal mapping's random walk reaches: NaN pixels,
+    reproduced bit for bit (NaN included). The opt-in horizon fix (not a
+    reference behaviour; the reference checker refuses it) keeps the image finite."""
+    import xitils_gb300.scenes as S
+    from xitils_gb300.scene import METAL
+    fixed = S.mfnm_at_scale(40, 40, 4, grid=33, n_boxes=0, normal_res=64, env_size=(64, 32))
+    plain = S.mfnm_at_scale(40, 40, 4, grid=33, n_boxes=0, normal_res=64, env_size=(64, 32))
+    plain.params = IntegratorParams()  # the reference's own defaults (no depth limit)
+    for m in plain.materials:
+        if m.kind == METAL:
+            m.f = m.f[:4]
+    a = load_scene(plain, "port").render_pcg(plain)
+    b = load_scene(plain, "reference").render_pcg(plain)
+    assert np.array_equal(a, b, equal_nan=True)
+    assert (~np.isfinite(a)).any()
+    f = load_scene(fixed, "port").render_pcg(fixed)
+    assert np.isfinite(f).all()
+    with pytest.raises(AssertionError):
+        load_scene(fixed, "reference")

@@ -96,6 +96,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_material_specular_fresnel": [P, C.c_float, C.POINTER(P)],
         "xgb_material_mf_normalmap": [P, P, C.POINTER(P)],
         "xgb_material_set_normalmap": [P, P],
+        "xgb_material_set_fixes": [P, C.c_uint32],
         "xgb_material_destroy": [P],
         "xgb_scene_create": [P, C.POINTER(P)],
         "xgb_scene_destroy": [P],
@@ -587,6 +588,8 @@ class GpuSceneBuilder:
             m = Diffuse(ctx, f[:3], t)
         elif kind == METAL:
             m = Metal(ctx, f[0], f[1:4], t)
+            if len(f) > 4 and f[4]:
+                ctx.check(ctx.lib.xgb_material_set_fixes(m.h, int(f[4])), "set_fixes")
         elif kind == GLOSSY:
             m = Glossy(ctx, f[:3], f[3])
         elif kind == GLOSSY_HIGHLIGHT:

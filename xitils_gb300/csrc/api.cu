@@ -447,6 +447,14 @@ xgb_status xgb_material_metal(xgb_ctx* ctx, float roughness, const float f0[3], 
     m->tex = roughness_tex;
     return XGB_OK;
 }
+xgb_status xgb_material_set_fixes(xgb_material* m, uint32_t fixes) {
+    if (!m) return XGB_INVALID_ARG;
+    if (fixes & ~(uint32_t)XGB_FIX_METAL_HORIZON) return fail(m->ctx, XGB_INVALID_ARG, "xgb_material_set_fixes: unknown fix");
+    if ((fixes & XGB_FIX_METAL_HORIZON) && m->m.kind != MAT_METAL)
+        return fail(m->ctx, XGB_INVALID_ARG, "xgb_material_set_fixes: the horizon fix applies to Metal");
+    m->m.flags = (int)fixes;
+    return XGB_OK;
+}
 xgb_status xgb_material_glossy(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out) {
     if (!finite3(albedo)) return fail(ctx, XGB_INVALID_ARG, "xgb_material_glossy: bad albedo");
     xgb_material* m;

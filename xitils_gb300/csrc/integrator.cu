@@ -210,9 +210,20 @@ __device__ __forceinline__ float luminance(V3 c) { return 0.2126f * c.x + 0.7152
 
 // Materials the learned proposal may sample: non-delta BSDFs whose bsdfCos and
 // getPDF are deterministic.
-__device__ __forceinline__ bool guidable(int kind) {
+__device__ __forceinline__ bool guidableBasic(int kind) {
     return kind == MAT_DIFFUSE || kind == MAT_METAL || kind == MAT_GLOSSY || kind == MAT_GLOSSY_CLAMPED ||
            kind == MAT_GLOSSY_HIGHLIGHT;
+}
+// Materials the learned proposal is mixed into. Microfacet normal mapping
+// qualifies over a non-specular base: its sampler reports the approximate
+// getPDF (MicrofacetBasedNormalMapping/Main.cpp:254-321) as its density, and the
+// one-sample MIS below weights its sample by that density's balance-heuristic
+// share, which keeps the estimator unbiased for any density the two branches
+// agree on (the weights of the two techniques still sum to one); bsdfCos is the
+// random walk's unbiased estimate.
+__device__ __forceinline__ bool guidable(const SceneDev& sc, const Material& m) {
+    if (m.kind == MAT_MF_NORMALMAP) return m.base >= 0 && guidableBasic(sc.materials[m.base].kind);
+    return guidableBasic(m.kind);
 }
 
 __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
@@ -350,7 +361,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                         V3 wi;
                         float pdf = pdfPrev;  // left untouched by materials that do not set it
                         V3 f;
-                        const bool guidedHere = rp.guided && guidable(mat.kind);
+                        const bool guidedHere = rp.guided && guidable(sc, mat);
                         VmfMixture mx;
                         float fcos = 0.0f;  // luminance of bsdfCos(wi) at a guided vertex
                         if (!guidedHere) {

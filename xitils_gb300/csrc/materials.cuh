@@ -66,9 +66,14 @@ __device__ __forceinline__ V3 skyRadiance(const SceneDev& sc, V3 wi) {
 }
 
 // ------------------------------------------------------------------- Metal --
+// horizon = the below-horizon fix (XGB_FIX_METAL_HORIZON; not the reference's
+// behaviour): no reflection when wo or wi lies below the shading normal and no
+// sample for wo below it (the reference divides by a clamped zero there, which
+// microfacet normal mapping's random walk reaches and turns into NaN).
 struct MetalD {  // Material.h:275-384
     float alpha;
     V3 f0;
+    bool horizon = false;
     __device__ V3 F(V3 eye, V3 h) const { return f0 + (V3(1.0f) - f0) * powf(1 - dot(eye, h), 5.0f); }
     __device__ float D(V3 x, V3 n) const {
         float alpha2 = alpha * alpha;
@@ -108,6 +113,7 @@ struct MetalD {  // Material.h:275-384
         return basis.toGlobal(Ne);
     }
     __device__ V3 bsdfCos(const Surface& s, V3 wi) const {
+        if (horizon && (dot(s.wo, s.sn) <= 0.0f || dot(wi, s.sn) <= 0.0f)) return V3(0.0f);
         V3 h = normalize(wi + s.wo);
         V3 Fr = F(s.wo, h);
         float Dv = D(h, s.sn);
@@ -115,13 +121,21 @@ struct MetalD {  // Material.h:275-384
         return Fr * Dv * G / clampPositive(4 * dot(s.wo, s.sn));
     }
     __device__ float pdf(const Surface& s, V3 wi) const {
+        if (horizon && (dot(s.wo, s.sn) <= 0.0f || dot(wi, s.sn) <= 0.0f)) return 0.0f;
         V3 h = normalize(wi + s.wo);
+        if (horizon && !(dot(s.sn, h) > 0.0f && dot(s.wo, h) > 0.0f)) return 0.0f;
         return DV(h, s.sn, s.wo) / (4 * dot(s.wo, h));
     }
     __device__ V3 evalAndSample(const Surface& s, Pcg& rng, V3* wi, float* p) const {
+        if (horizon && dot(s.wo, s.sn) <= 0.0f) {
+            *wi = s.sn;
+            *p = 0.0f;
+            return V3(0.0f);
+        }
         V3 h = sampleVNDF(s.wo, s.sn, rng);
         *wi = (2.0f * dot(s.wo, h)) * h - s.wo;
         *p = pdf(s, *wi);
+        if (horizon && !(*p > 0.0f)) return V3(0.0f);
         return bsdfCos(s, *wi) / *p;
     }
 };
@@ -180,7 +194,7 @@ __device__ __forceinline__ V3 bsdfCosBasic(const SceneDev& sc, const Material& m
     }
     case MAT_METAL: {
         float r = metalRoughness(sc, m, s);
-        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.bsdfCos(s, wi);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z), (m.flags & 1) != 0}.bsdfCos(s, wi);
     }
     case MAT_GLOSSY: return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false}.bsdfCos(s, wi);
     case MAT_GLOSSY_CLAMPED: return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, true}.bsdfCos(s, wi);
@@ -196,7 +210,7 @@ __device__ __forceinline__ float pdfBasic(const SceneDev& sc, const Material& m,
     case MAT_DIFFUSE: return clampPositive(dot(wi, s.sn)) / kPi;  // Material.h:78-81
     case MAT_METAL: {
         float r = metalRoughness(sc, m, s);
-        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.pdf(s, wi);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z), (m.flags & 1) != 0}.pdf(s, wi);
     }
     case MAT_GLOSSY: return GlossyD{V3(), m.sharpness, false}.pdf(s, wi);
     case MAT_GLOSSY_CLAMPED: return GlossyD{V3(), m.sharpness, true}.pdf(s, wi);
@@ -223,7 +237,7 @@ __device__ __forceinline__ V3 sampleBasic(const SceneDev& sc, const Material& m,
     }
     case MAT_METAL: {
         float r = metalRoughness(sc, m, s);
-        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z)}.evalAndSample(s, rng, wi, pdf);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z), (m.flags & 1) != 0}.evalAndSample(s, rng, wi, pdf);
     }
     case MAT_GLOSSY:
         return GlossyD{V3(m.albedo.x, m.albedo.y, m.albedo.z), m.sharpness, false}.evalAndSample(s, rng, wi, pdf);

@@ -108,7 +108,7 @@ struct __align__(16) Material {
     float sharpnessHL;
     float rate;
     float index;
-    float pad;
+    int flags;  // bit 0: Metal below-horizon fix (XGB_FIX_METAL_HORIZON)
 };
 
 struct TextureDev {

@@ -110,8 +110,11 @@ class SceneDesc:
     def diffuse(self, albedo, tex: int = -1, normalmap: int = -1) -> int:
         return self.add_material(DIFFUSE, albedo, tex=tex, normalmap=normalmap)
 
-    def metal(self, roughness: float, f0, rough_tex: int = -1, normalmap: int = -1) -> int:
-        return self.add_material(METAL, [roughness, *f0], tex=rough_tex, normalmap=normalmap)
+    def metal(self, roughness: float, f0, rough_tex: int = -1, normalmap: int = -1, horizon_fix: bool = False) -> int:
+        """Metal (GGX conductor); horizon_fix = the opt-in below-horizon fix
+        (XGB_FIX_METAL_HORIZON), which the reference does not have."""
+        f = [roughness, *f0] + ([1.0] if horizon_fix else [])
+        return self.add_material(METAL, f, tex=rough_tex, normalmap=normalmap)
 
     def emission(self, power) -> int:
         return self.add_material(EMISSION, power)
