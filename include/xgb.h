@@ -100,6 +100,10 @@ xgb_status xgb_material_metal(xgb_ctx* ctx, float roughness, const float f0[3], 
  * inf / NaN, which microfacet normal mapping's random walk over a Metal base
  * reaches). Applies to materials whose scene is built afterwards. */
 #define XGB_FIX_METAL_HORIZON 1u
+/* Scene-level fix (xgb_scene_set_fixes): XGB_FIX_DROP_NONFINITE skips a
+ * radiance contribution with an inf or NaN component instead of adding it to the
+ * film (the reference adds it, and one such sample turns the pixel to NaN). */
+#define XGB_FIX_DROP_NONFINITE 2u
 xgb_status xgb_material_set_fixes(xgb_material* material, uint32_t fixes);
 /* Glossy(albedo, sharpness) (Material.h:88-132). */
 xgb_status xgb_material_glossy(xgb_ctx* ctx, const float albedo[3], float sharpness, xgb_material** out);
@@ -324,6 +328,9 @@ xgb_status xgb_guide_train_steps(xgb_guide* guide, uint64_t* out);
  * xgb_guide_set_training; standard integrator only; the call then holds 16
  * bytes of device memory per camera path). guide = NULL turns guiding off. */
 xgb_status xgb_scene_set_guide(xgb_scene* scene, xgb_guide* guide, float bsdf_fraction, int train, float learning_rate);
+
+/* Opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE); 0 = reference behaviour. */
+xgb_status xgb_scene_set_fixes(xgb_scene* scene, uint32_t fixes);
 
 /* Scene::intersect / Scene::intersectAny (Scene.h:30-38) for host arrays of n
  * rays, float[n][7] = origin, direction, tMax. xgb_scene_intersect writes

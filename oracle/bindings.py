@@ -107,6 +107,9 @@ class CpuChecker:
         assert r == 0
         return r
 
+    def set_fixes(self, fixes):
+        assert self._call("set_fixes", C.c_int(fixes)) == 0, "set_fixes refused"
+
     def build(self):
         assert self._call("build") == 0
 

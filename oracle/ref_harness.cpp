@@ -257,6 +257,12 @@ int xref_set_sky(void* p, int type, const float* rgb, int tex) {
     return -1;
 }
 
+// The reference has no quirk fixes: only 0 is accepted.
+int xref_set_fixes(void* p, int fixes) {
+    (void)p;
+    return fixes == 0 ? 0 : -1;
+}
+
 int xref_build(void* p) {
     RefScene* s = (RefScene*)p;
     s->scene.buildAccelerationStructure();

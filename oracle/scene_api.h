@@ -46,6 +46,7 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \
     int P##set_sky(void* s, int type, const float* rgb, int tex);                                  \
+    int P##set_fixes(void* s, int fixes);                                                          \
     int P##build(void* s);                                                                         \
     int P##render_pcg(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_count,               \
                       uint32_t seed, int integrator, int max_depth, int rr_start, float rr_prob,   \

@@ -490,6 +490,7 @@ struct Scene {
     int skyType = ORC_SKY_NONE;
     V3 skyColor;
     int skyTex = -1;
+    int fixes = 0;  // opt-in quirk fixes of the render (xcpu_set_fixes)
     bool built = false;
 };
 
@@ -953,6 +954,13 @@ struct Params {
 const float kRayOffset = 0.00001f;     // PathTracer.h:254
 const float kShadowMargin = 0.0001f;   // PathTracer.h:257
 
+// radiance + c, or radiance alone when the drop-non-finite fix is on and c has
+// a non-finite component (the reference adds it, and the pixel becomes NaN).
+V3 addContribution(const Scene& sc, V3 radiance, V3 c) {
+    if ((sc.fixes & 2) && !(std::isfinite(c.x) && std::isfinite(c.y) && std::isfinite(c.z))) return radiance;
+    return radiance + c;
+}
+
 // Material::getAlbedo (Material.h:44-47, 83-85, 129-131, 168-170, 380-382):
 // Diffuse albedo (times its texture), Glossy albedo, GlossyWithHighLight its
 // base's albedo, Metal f0; every other material (the sandbox's GlossyClamped
@@ -979,7 +987,7 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = n
     int pathLength = 1;
     bool canSampleLight = !sc.lights.empty();
     if (!sceneIntersect(sc, ray, &isect)) {
-        if (sc.skyType != ORC_SKY_NONE) radiance = radiance + weight * skyRadiance(sc, ray.d);
+        if (sc.skyType != ORC_SKY_NONE) radiance = addContribution(sc, radiance, weight * skyRadiance(sc, ray.d));
         return radiance;
     }
     ++pathLength;
@@ -988,7 +996,7 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = n
         aov[0] = albedoOf(sc, *mat, isect);
         aov[1] = isect.n;
     }
-    if (mat->emissive()) radiance = radiance + weight * emission(*mat, -ray.d, isect.n);
+    if (mat->emissive()) radiance = addContribution(sc, radiance, weight * emission(*mat, -ray.d, isect.n));
     while (true) {
         // An emitter's evalAndSample returns zero (Material.h:400-402): the
         // reference ends the path after an NEE step whose contribution is
@@ -1019,10 +1027,10 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = n
                     } else {
                         mis = 1.0f;
                     }
-                    if (mis > 0.0f) radiance = radiance + weight * mis * f * emission(nm, -ray.d, next.n);
+                    if (mis > 0.0f) radiance = addContribution(sc, radiance, weight * mis * f * emission(nm, -ray.d, next.n));
                 }
             } else {
-                if (sc.skyType != ORC_SKY_NONE) radiance = radiance + weight * f * skyRadiance(sc, ray.d);
+                if (sc.skyType != ORC_SKY_NONE) radiance = addContribution(sc, radiance, weight * f * skyRadiance(sc, ray.d));
                 nextSampled = false;
             }
         }
@@ -1048,7 +1056,7 @@ V3 evalStandard(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = n
                 if (mis > 0.0f) {
                     float G = fabsf(dot(-sray.d, ls.sn)) / distSq;
                     const Material& lm = sc.materials[sc.objects[ls.object].material];
-                    radiance = radiance + weight * mis * sh.bsdfCos(mi, isect, rng, sray.d) * emission(lm, -sray.d, ls.n) * G / pl;
+                    radiance = addContribution(sc, radiance, weight * mis * sh.bsdfCos(mi, isect, rng, sray.d) * emission(lm, -sray.d, ls.n) * G / pl);
                 }
             }
         }
@@ -1082,7 +1090,7 @@ V3 evalNaive(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = null
                 aov[0] = albedoOf(sc, m, isect);
                 aov[1] = isect.n;
             }
-            if (m.emissive()) radiance = radiance + weight * emission(m, -ray.d, isect.n);
+            if (m.emissive()) radiance = addContribution(sc, radiance, weight * emission(m, -ray.d, isect.n));
             float pdf;
             weight = weight * sh.evalAndSample(sc.objects[isect.object].material, isect, rng, &wi, &pdf);
             if (isZero(weight)) break;
@@ -1090,7 +1098,7 @@ V3 evalNaive(const Scene& sc, const Params& P, Rng& rng, Ray ray, V3* aov = null
             ray.o = isect.p + kRayOffset * ray.d;
             ray.tMax = kInf;
         } else if (sc.skyType != ORC_SKY_NONE) {
-            radiance = radiance + clampPositive(weight * skyRadiance(sc, ray.d));
+            radiance = addContribution(sc, radiance, clampPositive(weight * skyRadiance(sc, ray.d)));
             break;
         } else {
             // The reference loops forever here (no sky, miss); a miss ends the path.
@@ -1199,6 +1207,13 @@ int xcpu_set_camera(void* s, const float* c2w, const float* c2wInv, float fov, f
     std::memcpy(sc->c2w.m, c2w, 64);
     std::memcpy(sc->c2wInv.m, c2wInv, 64);
     sc->fov = fov; sc->aspect = aspect;
+    return 0;
+}
+
+// Opt-in quirk fixes of the render (not reference behaviour): bit 1 drops a
+// radiance contribution with a non-finite component instead of adding it.
+int xcpu_set_fixes(void* s, int fixes) {
+    ((Scene*)s)->fixes = fixes;
     return 0;
 }
 

@@ -97,6 +97,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_material_mf_normalmap": [P, P, C.POINTER(P)],
         "xgb_material_set_normalmap": [P, P],
         "xgb_material_set_fixes": [P, C.c_uint32],
+        "xgb_scene_set_fixes": [P, C.c_uint32],
         "xgb_material_destroy": [P],
         "xgb_scene_create": [P, C.POINTER(P)],
         "xgb_scene_destroy": [P],
@@ -623,6 +624,9 @@ class GpuSceneBuilder:
 
     def set_sky(self, kind, rgb, tex):
         self.scene.setSky(kind, rgb, self.textures[tex] if tex >= 0 else None)
+
+    def set_fixes(self, fixes):
+        self.ctx.check(self.ctx.lib.xgb_scene_set_fixes(self.scene.h, fixes), "set_fixes")
 
     def build(self):
         self.scene.buildAccelerationStructure()

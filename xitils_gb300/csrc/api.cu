@@ -192,6 +192,7 @@ struct xgb_scene {
     float guideLr = 1e-3f;
     float4* mix = nullptr;  // per-path mixtures (capacity x 10 float4)
     unsigned int mixCapacity = 0;
+    unsigned int fixes = 0;     // opt-in quirk fixes (xgb_scene_set_fixes)
     float4* pathAcc = nullptr;  // guide training: per-path contributions of a call
     unsigned long long pathAccCapacity = 0;
     double vertsPerPath = 4.0;  // extension rays per path of the last call (sizes the record rate)
@@ -839,6 +840,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.nInstances = (int)inst.size();
     sd.tlasRootIsLeaf = tlasRootIsLeaf;
     sd.blasLayout = blasLayout;
+    sd.fixes = (int)s->fixes;
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;
@@ -1021,6 +1023,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.filmFp64 = film->fp64;
     rp.film = film->d;
     rp.aov = film->aov;
+    rp.dropNonFinite = (s->fixes & XGB_FIX_DROP_NONFINITE) ? 1 : 0;
     rp.guided = 0;
     rp.train = 0;
     rp.bsdfFrac = s->bsdfFrac;
@@ -1214,6 +1217,14 @@ xgb_status xgb_scene_intersect(xgb_scene* s, int n, const float* rays, float* hi
 
 xgb_status xgb_scene_occluded(xgb_scene* s, int n, const float* rays, int32_t* occluded, void* stream) {
     return sceneQuery(s, n, rays, 1, nullptr, occluded, stream);
+}
+
+xgb_status xgb_scene_set_fixes(xgb_scene* s, uint32_t fixes) {
+    if (!s) return XGB_INVALID_ARG;
+    if (fixes & ~(uint32_t)XGB_FIX_DROP_NONFINITE) return fail(s->ctx, XGB_INVALID_ARG, "xgb_scene_set_fixes: unknown fix");
+    s->fixes = fixes;
+    s->sd.fixes = (int)fixes;
+    return XGB_OK;
 }
 
 xgb_status xgb_scene_set_profiling(xgb_scene* s, int enable) {

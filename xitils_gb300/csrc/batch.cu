@@ -188,6 +188,7 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
         rp.capacity = o.queue_capacity;
         rp.filmFp64 = f64;
         rp.film = fd;
+        rp.dropNonFinite = (sd.fixes & XGB_FIX_DROP_NONFINITE) ? 1 : 0;
         b->hScenes[i] = sd;
         b->hParams[i] = rp;
         b->hStart[i] = total;

@@ -134,6 +134,7 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     rp.capacity = cap;
     rp.filmFp64 = fp64;
     rp.film = filmPtr;
+    rp.dropNonFinite = (sd.fixes & XGB_FIX_DROP_NONFINITE) ? 1 : 0;
 
     // The counters keep the previous call's values: start from zero.
     Ctrl host;

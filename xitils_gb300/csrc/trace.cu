@@ -12,6 +12,7 @@
 namespace xgb {
 
 __device__ __forceinline__ void filmAdd(const RenderParams& rp, int pix, V3 c) {
+    if (rp.dropNonFinite && !(isfinite(c.x) && isfinite(c.y) && isfinite(c.z))) return;
     if (rp.filmFp64) {
         double* f = (double*)rp.film + 4 * (size_t)pix;
         atomicAdd(f, (double)c.x);

@@ -114,6 +114,7 @@ struct RenderParams {
     int filmFp64;
     void* film;  // float4* or double4*
     void* aov;   // first-hit albedo plane then normal plane (same type as film), nullptr: off
+    int dropNonFinite;  // film additions with a non-finite component are skipped (opt-in fix)
     // learned proposal (0 / nullptr when off)
     int guided;
     int train;

@@ -136,6 +136,7 @@ struct SceneDev {
     int nInstances;
     int tlasRootIsLeaf;
     int blasLayout;  // every mesh binary (0), every mesh wide (1), or a mix (2)
+    int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;

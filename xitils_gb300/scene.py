@@ -88,6 +88,7 @@ class SceneDesc:
     height: int = 64
     spp: int = 1
     params: IntegratorParams = field(default_factory=IntegratorParams)
+    fixes: int = 0  # opt-in quirk fixes of the render (2 = drop non-finite contributions)
 
     # -- construction -----------------------------------------------------
     def add_texture(self, rgb: np.ndarray, clamp: bool = True, filter: bool = True) -> int:
@@ -165,5 +166,7 @@ class SceneDesc:
         backend.set_camera(c2w.mat, c2w.matInv, fov, aspect)
         kind, rgb, tex = self.sky
         backend.set_sky(kind, rgb, tex)
+        if self.fixes:
+            backend.set_fixes(self.fixes)
         backend.build()
         return backend

@@ -419,4 +419,5 @@ def mfnm_at_scale(width: int = 2048, height: int = 2048, spp: int = 256, grid: i
         s.add_object(s.add_mesh(lp, li), s.emission([30.0, 27.0, 22.0]))
     s.set_sky(SKY_LATLONG, tex=s.add_texture(latlong_sky(*env_size), clamp=True, filter=True))
     s.set_camera(look_at((0.5, 0.42, -0.25), (0.5, 0.02, 0.55), (0, 1, 0)), 50.0 * math.pi / 180.0, height / width)
+    s.fixes = 2  # samples the normal-mapping walk still turns non-finite (0/0 facet weights) are dropped
     return s
