@@ -58,26 +58,16 @@ def test_equal_time_harness_runs(room):
     assert np.isfinite(out["guided"]["relmse"])
 
 
-def test_guided_normal_mapping_is_unbiased(room):
-    """Guiding at microfacet-normal-mapped vertices (stochastic bsdfCos, approximate
-    getPDF as the BSDF technique's density): the guided image converges to the
-    plain one."""
+def test_guiding_leaves_normal_mapped_vertices_to_their_sampler(room):
+    """Microfacet-normal-mapped vertices are not guided (their sampler's density is
+    only approximated): with every surface normal-mapped, a guided render with
+    a trained network draws the same paths as the plain one."""
     api, guiding, ctx, _, _, _ = room
-    desc = scenes.mfnm_at_scale(48, 48, 1, grid=65, n_boxes=6, normal_res=64, env_size=(128, 64))
+    desc = scenes.mfnm_at_scale(32, 32, 4, grid=33, n_boxes=2, normal_res=64, env_size=(64, 32))
     b = api.load_scene(ctx, desc)
-    ref = guiding.render_reference(ctx, b, desc, 4096)
+    plain = api.render_desc(ctx, desc, builder=b)
     guide = api.Guide(ctx, seed=1)
-    guide.set_training(1024)
-    b.scene.setGuide(guide, 0.5, train=True, lr=1e-3)
-    scratch = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
-    for k in range(16):
-        scratch.render(b.scene, 1, desc.params, 5000 + k)
-    assert guide.steps() > 0
     b.scene.setGuide(guide, 0.5, train=False)
-    g = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
-    g.render(b.scene, 512, desc.params, 0)
+    guided = api.render_desc(ctx, desc, builder=b)
     b.scene.setGuide(None)
-    G = g.download() / 512
-    assert np.isfinite(G).all()
-    print("guided mean", G.mean(), "reference mean", ref.mean(), "relMSE", guiding.relmse(G, ref))
-    assert abs(G.mean() - ref.mean()) < 0.02 * ref.mean()
+    np.testing.assert_allclose(guided, plain, rtol=1e-5, atol=1e-5)
