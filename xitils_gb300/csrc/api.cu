@@ -193,6 +193,7 @@ struct xgb_scene {
     float4* mix = nullptr;  // per-path mixtures (capacity x 10 float4)
     unsigned int mixCapacity = 0;
     unsigned int fixes = 0;     // opt-in quirk fixes (xgb_scene_set_fixes)
+    bool guidable = false;      // some object's material takes the learned proposal
     float4* pathAcc = nullptr;  // guide training: per-path contributions of a call
     unsigned long long pathAccCapacity = 0;
     double vertsPerPath = 4.0;  // extension rays per path of the last call (sizes the record rate)
@@ -747,6 +748,13 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
         dm[i].normalmap = texId(mats[i]->normalmap);
         dm[i].base = mats[i]->base ? matIds[mats[i]->base] : -1;
     }
+    // whether any object's material takes the learned proposal (integrator.cu::guidableBasic)
+    s->guidable = false;
+    for (const Instance& in : inst) {
+        const int k = dm[in.material].kind;
+        if (k == MAT_DIFFUSE || k == MAT_METAL || k == MAT_GLOSSY || k == MAT_GLOSSY_CLAMPED || k == MAT_GLOSSY_HIGHLIGHT)
+            s->guidable = true;
+    }
     int skyTex = texId(s->skyTex);
     std::vector<TextureDev> td(texs.size());
     for (size_t i = 0; i < texs.size(); ++i) td[i] = TextureDev{texs[i]->d, texs[i]->w, texs[i]->h, texs[i]->clamp, texs[i]->filter};
@@ -1027,7 +1035,8 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.guided = 0;
     rp.train = 0;
     rp.bsdfFrac = s->bsdfFrac;
-    xgb_guide* gd = s->guide;
+    // a scene without guidable materials renders as plain (no inference, no records)
+    xgb_guide* gd = s->guidable ? s->guide : nullptr;
     GuideBounds gb;
     if (gd) {
         if (s->mixCapacity < cap) {
