@@ -62,7 +62,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="xgb", choices=["xgb", "reference"])
-    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell", "batch", "mfnm"])
+    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell", "shell", "batch", "mfnm"])
+    p.add_argument("--shell-grid", type=int, default=256)
     p.add_argument("--mfnm-res", type=int, default=2048)
     p.add_argument("--mfnm-ref-spp", type=int, default=2048)
     p.add_argument("--batch-scenes", type=int, default=64)
@@ -79,20 +80,41 @@ def parse():
     return p.parse_args()
 
 
+SINGLE_KERNEL = "k_trace_single (closest-hit traversal of a one-instance scene, binary BVH, persistent)"
+
+
 def make_workload(args):
+    """(scene, label, meta): meta names the data, the extension kernel the scene
+    runs and how the timed steps relate to L2."""
     from xitils_gb300 import scenes
+    big = "inputs larger than L2 (BVH + triangles exceed 129 MB)"
     if args.workload == "terrain":
         res = args.res or 1024
         spp = args.spp or 64
         desc = scenes.terrain(grid=args.grid, width=res, height=res, spp=spp, max_depth=10)
         label = (f"terrain {args.grid}x{args.grid} grid ({desc.n_tris} tris), {res}x{res} film, {spp} spp, "
                  f"max depth 10, GGX per-texel roughness, lat-long env 1024x512")
+        meta = {"data": "synthetic (seeded fBm terrain, procedural lat-long environment)", "kernel": SINGLE_KERNEL,
+                "l2": big}
+    elif args.workload == "shell":
+        res = args.res or 1024
+        spp = args.spp or 16
+        grid = args.shell_grid
+        desc = scenes.shell_fabric(res, res, spp, grid=grid, layers=16, tex_res=1024)
+        label = (f"shell-mapped fabric: {grid}x{grid} cloth grid x 16 layers ({desc.n_tris} tris), 1024^2 weave "
+                 f"displacement map, Cornell-style room, {res}x{res} film, {spp} spp, reference defaults "
+                 f"(no depth limit, RR after 5 at 0.9)")
+        meta = {"data": "synthetic (seeded cloth patch, procedural plain-weave displacement map)",
+                "kernel": "k_extend (two-level closest-hit traversal with the shell-mapping discard, persistent)",
+                "l2": big}
     else:
         res = args.res or 512
         spp = args.spp or 16
         desc = scenes.cornell(res, res, spp)
         label = f"cornell 36 tris, {res}x{res} film, {spp} spp, max depth 8, RR after depth 3"
-    return desc, label
+        meta = {"data": "synthetic (the Cornell box of the workload description)", "kernel": SINGLE_KERNEL,
+                "l2": "the scene fits in L2 (36 triangles); path queues of 2^21 paths stream through HBM"}
+    return desc, label, meta
 
 
 class ClockSampler:
@@ -183,7 +205,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    desc, label = make_workload(args)
+    desc, label, meta = make_workload(args)
     res, spp = args.cpu_sample_res, 1
     nthreads = os.cpu_count() or 1
     from oracle.bindings import CpuChecker
@@ -205,7 +227,7 @@ def run_reference(args):
         "impl": "reference", "metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded fBm terrain, procedural lat-long environment)",
+        "data": meta["data"],
         "config": {"workload": label, "sample_per_step": f"{res}x{res} film x {spp} spp of the same scene and camera",
                    "integrator": "reference StandardPathTracer defaults (no depth limit, RR after length 5)"},
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": nthreads, "kind": kind,
@@ -360,7 +382,7 @@ def run_xgb(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    desc, label = make_workload(args)
+    desc, label, meta = make_workload(args)
     ctx = api.Context(local)
     builder = api.load_scene(ctx, desc)
     scene = builder.scene
@@ -439,7 +461,7 @@ def run_xgb(args):
     ext_launches = max(stage_launch[2], 1)
     achieved = EXTEND_BYTES_PER_RAY * agg["extension_rays"] / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
     roofline = {
-        "kernel": "k_trace_single (closest-hit traversal of a one-instance scene, binary BVH, persistent)",
+        "kernel": meta["kernel"],
         "bound": "hbm",
         "achieved": achieved,
         "peak": hbm if hbm else 6800.0,
@@ -479,9 +501,9 @@ def run_xgb(args):
         "metric": "Mpaths/s", "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded fBm terrain, procedural lat-long environment)",
+        "data": meta["data"],
         "config": {"workload": label, "parallelism": f"replicas x{world} (disjoint sample ranges)",
-                   "l2": "inputs larger than L2 (BVH + triangles exceed 129 MB)",
+                   "l2": meta["l2"],
                    "queue_capacity": 1 << 21},
         "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC),
                 "d2h_bytes_per_step": W * H * 12},

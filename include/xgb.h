@@ -84,6 +84,23 @@ xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* position
                            int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out);
 xgb_status xgb_mesh_destroy(xgb_mesh* mesh);
 xgb_status xgb_mesh_triangle_count(const xgb_mesh* mesh, int* out);
+/* TriangleMesh::setGeometryWithShellMapping(vertexNum, positions, texCoords,
+ * normals, tangents, bitangents, indexNum, indices, displacement, scale,
+ * layerNum) (Include/Xitils/TriangleMesh.h:163-177, :279-324): layer_count
+ * copies of the mesh, copy l offset along the vertex normals by
+ * scale * l / (layer_count - 1); a hit on copy l is discarded where the red
+ * channel of the displacement texture at the hit's texcoord is below
+ * l / (layer_count - 1), for closest-hit and any-hit rays alike, and a kept
+ * hit's shading normal is tilted by the texture's central differences
+ * (TriangleIndexedWithShellMapping, TriangleIndexed.h:220-256). Every
+ * attribute array is required (the reference replicates all of them). The
+ * displacement texture must outlive the mesh. The mesh has
+ * layer_count x index_count / 3 triangles. */
+xgb_status xgb_mesh_create_shell(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                                 const float* normals, const float* tangents, const float* bitangents,
+                                 int vec3_stride, int uv_stride, int index_count, const int32_t* indices,
+                                 const xgb_texture* displacement, float displacement_scale, int layer_count,
+                                 xgb_mesh** out);
 
 /* --------------------------------------------------------------- materials */
 /* Diffuse(albedo) (Include/Xitils/Material.h:50-86); albedo_tex optional (Diffuse::texture). */

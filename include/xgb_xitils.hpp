@@ -4,6 +4,7 @@
 // It mirrors the reference's construction and render calls so that a sandbox
 // switches by changing namespaces:
 //   xitils::TriangleMesh::setGeometry  (Include/Xitils/TriangleMesh.h:151-161) -> xgb::TriangleMesh::setGeometry
+//   xitils::TriangleMesh::setGeometryWithShellMapping (TriangleMesh.h:163-177) -> the same name
 //   xitils::Object(shape, material, T) (Include/Xitils/Object.h:32-34)         -> xgb::Object
 //   xitils::Scene::addObject / buildAccelerationStructure (Scene.h:17-28)     -> xgb::Scene
 //   xitils::PinholeCamera(T, fov, aspect) (Camera.h:32-36)                     -> xgb::PinholeCamera
@@ -88,12 +89,26 @@ public:
                               uvStride, indexNum, indexData, &h_),
               ctx_, "TriangleMesh::setGeometry");
     }
+    // xitils::TriangleMesh::setGeometryWithShellMapping (TriangleMesh.h:163-177): the mesh
+    // keeps the displacement texture alive.
+    void setGeometryWithShellMapping(int vertexNum, const float* positions, const float* texCoords,
+                                     const float* normals, const float* tangents, const float* bitangents,
+                                     int indexNum, const int* indexData, std::shared_ptr<const Texture> displacement,
+                                     float displacementScale, int layerNum, int vec3Stride = 16, int uvStride = 16) {
+        if (h_) { xgb_mesh_destroy(h_); h_ = nullptr; }
+        displacement_ = displacement;
+        check(xgb_mesh_create_shell(ctx_, vertexNum, positions, texCoords, normals, tangents, bitangents, vec3Stride,
+                                    uvStride, indexNum, indexData, displacement ? displacement->get() : nullptr,
+                                    displacementScale, layerNum, &h_),
+              ctx_, "TriangleMesh::setGeometryWithShellMapping");
+    }
     int triangleNum() const { int n = 0; if (h_) xgb_mesh_triangle_count(h_, &n); return n; }
     const xgb_mesh* get() const { return h_; }
 
 private:
     xgb_ctx* ctx_;
     xgb_mesh* h_ = nullptr;
+    std::shared_ptr<const Texture> displacement_;
 };
 
 class Material {

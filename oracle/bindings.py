@@ -79,6 +79,15 @@ class CpuChecker:
         assert r >= 0, "add_mesh failed"
         return r
 
+    def add_mesh_shell(self, pos, idx, uv, nrm, tan, bit, tex, scale, layers):
+        arrs = [_fptr(a) for a in (pos, uv, nrm, tan, bit)]
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        self._keep.extend([a[0] for a in arrs] + [idx])
+        r = self._call("add_mesh_shell", C.c_int(len(pos)), *[a[1] for a in arrs], C.c_int(idx.size),
+                       idx.ctypes.data_as(C.POINTER(C.c_int32)), C.c_int(tex), C.c_float(scale), C.c_int(layers))
+        assert r >= 0, "add_mesh_shell failed"
+        return r
+
     def add_material(self, kind, f, base=-1, tex=-1, normalmap=-1):
         fa = np.zeros(16, dtype=np.float32)
         fa[:len(f)] = f

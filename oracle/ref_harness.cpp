@@ -182,6 +182,23 @@ int xref_add_mesh(void* p, int nV, const float* pos, const float* uv, const floa
     return (int)s->meshes.size() - 1;
 }
 
+// The reference's own TriangleMesh::setGeometryWithShellMapping (TriangleMesh.h:163-177).
+// Every attribute is required: the reference replicates each array per layer.
+int xref_add_mesh_shell(void* p, int nV, const float* pos, const float* uv, const float* nrm, const float* tan,
+                        const float* bit, int nIdx, const int32_t* idx, int tex, float scale, int layers) {
+    RefScene* s = (RefScene*)p;
+    if (!uv || !nrm || !tan || !bit || layers < 1 || tex < 0 || tex >= (int)s->textures.size()) return -1;
+    std::vector<Vector3f> P = toV3(pos, nV), N = toV3(nrm, nV), T = toV3(tan, nV), B = toV3(bit, nV);
+    std::vector<Vector2f> UV(nV);
+    for (int i = 0; i < nV; ++i) UV[i] = Vector2f(uv[2 * i], uv[2 * i + 1]);
+    std::vector<int> I(idx, idx + nIdx);
+    auto mesh = std::make_shared<TriangleMesh>();
+    mesh->setGeometryWithShellMapping(nV, P.data(), UV.data(), N.data(), T.data(), B.data(), nIdx, I.data(),
+                                      s->textures[tex], scale, layers);
+    s->meshes.push_back(mesh);
+    return (int)s->meshes.size() - 1;
+}
+
 int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
     RefScene* s = (RefScene*)p;
     std::shared_ptr<Material> m;

@@ -42,6 +42,9 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
     int P##add_texture(void* s, int w, int h, const float* rgb, int wrap_clamp, int filter);       \
     int P##add_mesh(void* s, int nV, const float* pos, const float* uv, const float* nrm,          \
                     const float* tan, const float* bit, int nIdx, const int32_t* idx);             \
+    int P##add_mesh_shell(void* s, int nV, const float* pos, const float* uv, const float* nrm,    \
+                          const float* tan, const float* bit, int nIdx, const int32_t* idx,        \
+                          int tex, float scale, int layers);                                       \
     int P##add_material(void* s, int type, const float* f, int base, int tex, int normalmap);      \
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \

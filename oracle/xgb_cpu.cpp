@@ -177,6 +177,37 @@ struct Texture {
         int y = (int)(uv.y * h);
         return at(x, y);
     }
+    // Texture.h:105-111: central differences scaled by the size
+    V3 diffUAt(int x, int y) const { return (at(x + 1, y) - at(x - 1, y)) / 2.0f * (float)w; }
+    V3 diffVAt(int x, int y) const { return (at(x, y + 1) - at(x, y - 1)) / 2.0f * (float)h; }
+    // Texture.h:113-132: rows addressed from 1 - v
+    V3 diffU(V2 uv) const {
+        if (filter) {
+            int x0 = (int)floorf(uv.x * w - 0.5f);
+            int y0 = (int)floorf((1 - uv.y) * h - 0.5f);
+            int x1 = x0 + 1, y1 = y0 + 1;
+            float wx1 = (uv.x * w - 0.5f) - x0;
+            float wy1 = ((1 - uv.y) * h - 0.5f) - y0;
+            float wx0 = 1.0f - wx1, wy0 = 1.0f - wy1;
+            return wx0 * wy0 * diffUAt(x0, y0) + wx0 * wy1 * diffUAt(x0, y1) + wx1 * wy0 * diffUAt(x1, y0) +
+                   wx1 * wy1 * diffUAt(x1, y1);
+        }
+        return diffUAt((int)(uv.x * w), (int)((1 - uv.y) * h));
+    }
+    // Texture.h:135-155: rows addressed from v
+    V3 diffV(V2 uv) const {
+        if (filter) {
+            int x0 = (int)floorf(uv.x * w - 0.5f);
+            int y0 = (int)floorf(uv.y * h - 0.5f);
+            int x1 = x0 + 1, y1 = y0 + 1;
+            float wx1 = (uv.x * w - 0.5f) - x0;
+            float wy1 = (uv.y * h - 0.5f) - y0;
+            float wx0 = 1.0f - wx1, wy0 = 1.0f - wy1;
+            return wx0 * wy0 * diffVAt(x0, y0) + wx0 * wy1 * diffVAt(x0, y1) + wx1 * wy0 * diffVAt(x1, y0) +
+                   wx1 * wy1 * diffVAt(x1, y1);
+        }
+        return diffVAt((int)(uv.x * w), (int)(uv.y * h));
+    }
 };
 
 // --------------------------------------------------------------- geometry --
@@ -341,6 +372,10 @@ struct Mesh {
     std::vector<float> triArea;  // TriangleIndexed::surfaceArea, TriangleIndexed.h:56-62
     float area = 0;               // TriangleMesh::calcSurfaceArea, TriangleMesh.h:253-258
     Bvh bvh;
+    // shell mapping (TriangleMesh.h:279-324): triangle t is face t % shellFaces on layer t / shellFaces
+    int shellLayers = 0, shellFaces = 0;
+    float shellScale = 0;
+    Texture shellTex;
 
     V3 p(int t, int k) const { return pos[idx[t * 3 + k]]; }
 
@@ -411,9 +446,17 @@ bool intersectTriangle(const Mesh& m, int tri, const Ray& ray, float* tHit, Isec
     float invDet = 1 / det;
     float b0 = e0 * invDet, b1 = e1 * invDet;
     float t = tScaled * invDet;
-    if (!is) { *tHit = t; return true; }
     int i0 = m.idx[tri * 3], i1 = m.idx[tri * 3 + 1], i2 = m.idx[tri * 3 + 2];
-    is->uv = m.uv.empty() ? V2() : lerp3(m.uv[i0], m.uv[i1], m.uv[i2], b0, b1);
+    V2 uv = m.uv.empty() ? V2() : lerp3(m.uv[i0], m.uv[i1], m.uv[i2], b0, b1);
+    // TriangleIndexedWithShellMapping::discardByAlpha (TriangleIndexed.h:233-235) with
+    // height = layer / (layerNum - 1) (TriangleMesh.h:316); any-hit queries too
+    // (Geometry::intersectAny calls intersect, Geometry.h:16-20).
+    if (m.shellLayers) {
+        float height = (float)(tri / m.shellFaces) / (m.shellLayers - 1);
+        if (m.shellTex.lookup(uv).x < height) return false;
+    }
+    if (!is) { *tHit = t; return true; }
+    is->uv = uv;
     *tHit = t;
     is->p = lerp3(p0, p1, p2, b0, b1);
     is->wo = normalize(-ray.d);
@@ -430,6 +473,16 @@ bool intersectTriangle(const Mesh& m, int tri, const Ray& ray, float* tHit, Isec
     is->sbitangent = is->bitangent;
     is->sn = faceForward(is->sn, is->wo);
     is->tri = tri;
+    if (m.shellLayers) {  // TriangleIndexedWithShellMapping::perturbIntersection (TriangleIndexed.h:237-254)
+        V3 a;
+        a.x = -m.shellTex.diffU(is->uv).x * m.shellScale;
+        a.y = -m.shellTex.diffV(is->uv).x * m.shellScale;
+        a.z = 1;
+        a = normalize(a);
+        is->sn = normalize(a.x * is->stangent + a.y * is->sbitangent + a.z * is->sn);
+        is->stangent = V3();
+        is->sbitangent = V3();
+    }
     return true;
 }
 
@@ -1159,6 +1212,47 @@ int xcpu_add_mesh(void* s, int nV, const float* pos, const float* uv, const floa
     if (uv) { m.uv.resize(nV); for (int i = 0; i < nV; ++i) m.uv[i] = V2(uv[2 * i], uv[2 * i + 1]); }
     if (!m.tan.empty() && m.bit.empty()) return -1;
     m.idx.assign(idx, idx + nIdx);
+    m.build();
+    sc->meshes.push_back(std::move(m));
+    return (int)sc->meshes.size() - 1;
+}
+
+// TriangleMesh::setGeometryWithShellMapping (TriangleMesh.h:163-177) and
+// buildTrianglesWithShellMapping (:279-324).
+int xcpu_add_mesh_shell(void* s, int nV, const float* pos, const float* uv, const float* nrm, const float* tan,
+                        const float* bit, int nIdx, const int32_t* idx, int tex, float scale, int layers) {
+    Scene* sc = (Scene*)s;
+    if (nV <= 0 || !pos || !uv || !nrm || !tan || !bit || nIdx <= 0 || nIdx % 3 || !idx || layers < 1) return -1;
+    if (tex < 0 || tex >= (int)sc->textures.size()) return -1;
+    for (int i = 0; i < nIdx; ++i) if (idx[i] < 0 || idx[i] >= nV) return -1;
+    Mesh m;
+    const size_t V = (size_t)nV;
+    m.pos.resize(V * layers); m.nrm.resize(V * layers); m.tan.resize(V * layers); m.bit.resize(V * layers);
+    m.uv.resize(V * layers);
+    for (size_t i = 0; i < V; ++i) {
+        m.pos[i] = V3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        m.nrm[i] = V3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+        m.tan[i] = V3(tan[3 * i], tan[3 * i + 1], tan[3 * i + 2]);
+        m.bit[i] = V3(bit[3 * i], bit[3 * i + 1], bit[3 * i + 2]);
+        m.uv[i] = V2(uv[2 * i], uv[2 * i + 1]);
+    }
+    m.idx.resize((size_t)nIdx * layers);
+    for (int i = 0; i < nIdx; ++i) m.idx[i] = idx[i];
+    for (int layer = 1; layer < layers; ++layer) {
+        for (size_t i = 0; i < V; ++i) {
+            float d = scale * layer / (layers - 1);
+            m.pos[layer * V + i] = m.pos[i] + d * m.nrm[i];
+            m.uv[layer * V + i] = m.uv[i];
+            m.nrm[layer * V + i] = m.nrm[i];
+            m.tan[layer * V + i] = m.tan[i];
+            m.bit[layer * V + i] = m.bit[i];
+        }
+        for (int i = 0; i < nIdx; ++i) m.idx[(size_t)layer * nIdx + i] = idx[i] + layer * nV;
+    }
+    m.shellLayers = layers;
+    m.shellFaces = nIdx / 3;
+    m.shellScale = scale;
+    m.shellTex = sc->textures[tex];
     m.build();
     sc->meshes.push_back(std::move(m));
     return (int)sc->meshes.size() - 1;

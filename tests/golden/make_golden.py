@@ -32,6 +32,7 @@ CASES = {
     "simple_path_tracer_48x48x4": (lambda: scenes.simple_path_tracer_scene(48, 48, 4), IntegratorParams()),
     "terrain_g65_40x40x2": (lambda: scenes.terrain(grid=65, width=40, height=40, spp=2, env_size=(128, 64)),
                             IntegratorParams()),
+    "shell_fabric_g24_40x40x2": (lambda: scenes.shell_fabric(40, 40, 2, grid=24, tex_res=64), IntegratorParams()),
 }
 
 
@@ -41,6 +42,7 @@ AOV_CASES = {
     "zoo_latlong_40x40x2": (lambda: scenes.material_zoo(40, 40, 2, sky="latlong"), IntegratorParams()),
     "terrain_g65_32x32x2": (lambda: scenes.terrain(grid=65, width=32, height=32, spp=2, env_size=(128, 64)),
                             IntegratorParams()),
+    "shell_fabric_g24_32x32x2": (lambda: scenes.shell_fabric(32, 32, 2, grid=24, tex_res=64), IntegratorParams()),
 }
 
 

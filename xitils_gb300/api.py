@@ -83,6 +83,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_texture_create": [P, C.c_int, C.c_int, C.c_int, FP, C.c_int, C.c_int, C.POINTER(P)],
         "xgb_texture_destroy": [P],
         "xgb_mesh_create": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(P)],
+        "xgb_mesh_create_shell": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), P,
+                                  C.c_float, C.c_int, C.POINTER(P)],
         "xgb_mesh_destroy": [P],
         "xgb_mesh_triangle_count": [P, C.POINTER(C.c_int)],
         "xgb_material_diffuse": [P, FP, P, C.POINTER(P)],
@@ -233,6 +235,25 @@ class TriangleMesh:
                                           idx.size, idx.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(self.h)),
                   "TriangleMesh.setGeometry")
         self.n_tris = idx.size // 3
+        return self
+
+    def setGeometryWithShellMapping(self, positions, texCoords, normals, tangents, bitangents, indices,
+                                    displacement: "Texture", displacementScale: float, layerNum: int):
+        """TriangleMesh::setGeometryWithShellMapping (TriangleMesh.h:163-177):
+        layerNum copies offset along the normals, hits discarded below the
+        displacement's height; every attribute array is required."""
+        pos = _f32(positions).reshape(-1, 3)
+        uv, n, t, b = (_f32(a).reshape(-1, k) for a, k in ((texCoords, 2), (normals, 3), (tangents, 3),
+                                                           (bitangents, 3)))
+        idx = np.ascontiguousarray(np.asarray(indices, dtype=np.int32).reshape(-1))
+        self.h = P()
+        self.displacement = displacement  # the library keeps a reference to the texture's device data
+        ctx = self.ctx
+        ctx.check(ctx.lib.xgb_mesh_create_shell(ctx.h, pos.shape[0], _fp(pos), _fp(uv), _fp(n), _fp(t), _fp(b), 12, 8,
+                                                idx.size, idx.ctypes.data_as(C.POINTER(C.c_int32)), displacement.h,
+                                                C.c_float(displacementScale), int(layerNum), C.byref(self.h)),
+                  "TriangleMesh.setGeometryWithShellMapping")
+        self.n_tris = idx.size // 3 * int(layerNum)
         return self
 
 
@@ -580,6 +601,11 @@ class GpuSceneBuilder:
 
     def add_mesh(self, pos, idx, uv=None, nrm=None, tan=None, bit=None):
         self.meshes.append(TriangleMesh(self.ctx).setGeometry(pos, uv, nrm, tan, bit, idx))
+        return len(self.meshes) - 1
+
+    def add_mesh_shell(self, pos, idx, uv, nrm, tan, bit, tex, scale, layers):
+        self.meshes.append(TriangleMesh(self.ctx).setGeometryWithShellMapping(pos, uv, nrm, tan, bit, idx,
+                                                                             self.textures[tex], scale, layers))
         return len(self.meshes) - 1
 
     def add_material(self, kind, f, base=-1, tex=-1, normalmap=-1):

@@ -120,6 +120,10 @@ struct xgb_mesh {
     std::vector<float> triArea;  // TriangleIndexed::surfaceArea
     float area = 0;              // TriangleMesh::calcSurfaceArea
     Box bound;                   // TriangleMesh::bound over all vertices
+    // shell mapping (xgb_mesh_create_shell): layers of shellFaces triangles each
+    const xgb_texture* shellTex = nullptr;
+    float shellScale = 0.0f;
+    int shellLayers = 0, shellFaces = 0;
 };
 
 struct xgb_material {
@@ -313,9 +317,9 @@ static void freeMesh(xgb_mesh* m) {
         dfree(p);
 }
 
-xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
-                           const float* normals, const float* tangents, const float* bitangents, int vec3_stride,
-                           int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out) {
+static xgb_status createMesh(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                             const float* normals, const float* tangents, const float* bitangents, int vec3_stride,
+                             int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out) {
     if (!ctx || !out) return XGB_INVALID_ARG;
     if (vertex_count <= 0 || !positions || index_count <= 0 || index_count % 3 || !indices)
         return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create: need positions and a multiple of 3 indices");
@@ -397,6 +401,69 @@ xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* position
         return e == cudaErrorMemoryAllocation ? fail(ctx, XGB_OOM, "xgb_mesh_create: out of device memory")
                                               : cudaFail(ctx, e, "xgb_mesh_create");
     }
+    *out = m;
+    return XGB_OK;
+}
+
+xgb_status xgb_mesh_create(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                           const float* normals, const float* tangents, const float* bitangents, int vec3_stride,
+                           int uv_stride, int index_count, const int32_t* indices, xgb_mesh** out) {
+    return createMesh(ctx, vertex_count, positions, texcoords, normals, tangents, bitangents, vec3_stride, uv_stride,
+                      index_count, indices, out);
+}
+
+// TriangleMesh::setGeometryWithShellMapping + buildTrianglesWithShellMapping
+// (TriangleMesh.h:163-177, :279-324): the vertex arrays repeated layer_count
+// times, layer l's positions moved by d = scale * l / (layer_count - 1) along
+// the vertex normals (in float, unfused: this file is compiled without FP
+// contraction), layer l's indices shifted by l * vertex_count. Triangle
+// l * faces + f of the result is face f on layer l.
+xgb_status xgb_mesh_create_shell(xgb_ctx* ctx, int vertex_count, const float* positions, const float* texcoords,
+                                 const float* normals, const float* tangents, const float* bitangents,
+                                 int vec3_stride, int uv_stride, int index_count, const int32_t* indices,
+                                 const xgb_texture* displacement, float displacement_scale, int layer_count,
+                                 xgb_mesh** out) {
+    if (!ctx || !out) return XGB_INVALID_ARG;
+    if (!positions || !texcoords || !normals || !tangents || !bitangents || !indices || !displacement)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: every vertex attribute and the displacement texture are required");
+    if (vertex_count <= 0 || index_count <= 0 || index_count % 3 || layer_count < 1 || !std::isfinite(displacement_scale))
+        return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: bad sizes, layer count or scale");
+    if ((int64_t)vertex_count * layer_count > INT32_MAX / 2 || (int64_t)index_count * layer_count > INT32_MAX / 2)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: too many layers for this mesh");
+    if (vec3_stride != 12 && vec3_stride != 16) return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: vec3_stride must be 12 or 16");
+    if (uv_stride != 8 && uv_stride != 16) return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: uv_stride must be 8 or 16");
+    const int vs = vec3_stride / 4, us = uv_stride / 4;
+    const size_t V = (size_t)vertex_count, L = (size_t)layer_count, I = (size_t)index_count;
+    std::vector<float> P(3 * V * L), N(3 * V * L), T(3 * V * L), B(3 * V * L), UV(2 * V * L);
+    std::vector<int32_t> idx(I * L);
+    for (size_t l = 0; l < L; ++l) {
+        // layer 0 keeps the input positions; the reference's loop starts at layer 1
+        const float d = l == 0 ? 0.0f : displacement_scale * (float)l / (float)(layer_count - 1);
+        for (size_t i = 0; i < V; ++i) {
+            const size_t o = l * V + i;
+            for (int c = 0; c < 3; ++c) {
+                const float p = positions[vs * i + c], n = normals[vs * i + c];
+                P[3 * o + c] = l == 0 ? p : p + d * n;
+                N[3 * o + c] = n;
+                T[3 * o + c] = tangents[vs * i + c];
+                B[3 * o + c] = bitangents[vs * i + c];
+            }
+            UV[2 * o] = texcoords[us * i];
+            UV[2 * o + 1] = texcoords[us * i + 1];
+        }
+        for (size_t k = 0; k < I; ++k) idx[l * I + k] = indices[k] + (int32_t)(l * V);
+    }
+    for (size_t k = 0; k < I; ++k)
+        if (indices[k] < 0 || indices[k] >= vertex_count)
+            return fail(ctx, XGB_INVALID_ARG, "xgb_mesh_create_shell: index out of range");
+    xgb_mesh* m = nullptr;
+    xgb_status st = createMesh(ctx, (int)(V * L), P.data(), UV.data(), N.data(), T.data(), B.data(), 12, 8,
+                               (int)(I * L), idx.data(), &m);
+    if (st != XGB_OK) return st;
+    m->shellTex = displacement;
+    m->shellScale = displacement_scale;
+    m->shellLayers = layer_count;
+    m->shellFaces = index_count / 3;
     *out = m;
     return XGB_OK;
 }
@@ -759,11 +826,22 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     std::vector<TextureDev> td(texs.size());
     for (size_t i = 0; i < texs.size(); ++i) td[i] = TextureDev{texs[i]->d, texs[i]->w, texs[i]->h, texs[i]->clamp, texs[i]->filter};
     std::vector<MeshDev> md(meshes.size());
-    int nWideMeshes = 0;
+    int nWideMeshes = 0, anyShell = 0;
     for (size_t i = 0; i < meshes.size(); ++i) {
         const xgb_mesh* m = meshes[i];
         md[i] = MeshDev{m->dNodes2, m->dNodes, m->wide, m->dTris, m->dPos, m->dUV, m->dNrm, m->dTan, m->dBit, m->dIdx,
                         m->dGnrm, m->dArea, m->nTris, m->nV, m->rootIsLeaf, m->rootLeaf};
+        if (m->shellTex) {
+            md[i].shellLayers = m->shellLayers;
+            md[i].shellFaces = m->shellFaces;
+            md[i].shellScale = m->shellScale;
+            md[i].shellTexels = m->shellTex->d;
+            md[i].shellW = m->shellTex->w;
+            md[i].shellH = m->shellTex->h;
+            md[i].shellClamp = m->shellTex->clamp;
+            md[i].shellFilter = m->shellTex->filter;
+            anyShell = 1;
+        }
         nWideMeshes += m->wide;
     }
     const int blasLayout = nWideMeshes == 0 ? 0 : (nWideMeshes == (int)meshes.size() ? 1 : 2);
@@ -849,6 +927,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.tlasRootIsLeaf = tlasRootIsLeaf;
     sd.blasLayout = blasLayout;
     sd.fixes = (int)s->fixes;
+    sd.shell = anyShell;
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;
@@ -1330,12 +1409,9 @@ xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
     g.w.W[3] = (__nv_bfloat16*)A(2 * kGuideOutPad * 64);
     g.w.WT[3] = (__nv_bfloat16*)A(2 * 64 * kGuideOutPad);
     g.w.bias[3] = (float*)A(4 * kGuideOutPad);
-    for (int l = 0; l < 4; ++l) g.scratch.X[l] = (__nv_bfloat16*)A(2 * (size_t)R * 64);
-    g.scratch.dirw = (float4*)A(16 * (size_t)R);
+    g.scratch.X0 = (__nv_bfloat16*)A(2 * (size_t)R * 64);
     g.scratch.Y = (float*)A(4 * (size_t)R * kGuideOutPad);
-    g.scratch.dY3 = (__nv_bfloat16*)A(2 * (size_t)R * kGuideOutPad);
-    for (int l = 0; l < 3; ++l) g.scratch.dZ[l] = (__nv_bfloat16*)A(2 * (size_t)R * 64);
-    g.scratch.dW = (float*)A(4 * (3 * 64 * 64 + kGuideOutPad * 64 + 256));
+    g.scratch.partial = (float*)A(guidePartialBytes());
     g.scratch.scalars = (float*)A(16);
     gd->arenaCap = 1 << 20;
     gd->arena = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)gd->arenaCap);
@@ -1452,8 +1528,8 @@ xgb_status xgb_guide_infer(xgb_guide* gd, int n, const float* pos, const float* 
         cudaMemcpyAsync(dIn, pos + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(dIn + 3 * R, nrm + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(dIn + 6 * R, wo + 3 * (size_t)b, 12 * (size_t)cnt, cudaMemcpyHostToDevice, st);
-        guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, cnt, rows, gd->bounds, gd->g.scratch.X[0], st);
-        guideInferRows(gd->g, gd->g.scratch.X[0], rows, gd->g.scratch.Y, st);
+        guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, cnt, rows, gd->bounds, gd->g.scratch.X0, st);
+        guideInferRows(gd->g, gd->g.scratch.X0, rows, gd->g.scratch.Y, st);
         cudaMemcpyAsync(y.data(), gd->g.scratch.Y, 4 * (size_t)rows * kGuideOutPad, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) {
             cudaFree(dIn);
@@ -1481,8 +1557,8 @@ xgb_status xgb_guide_sample(xgb_guide* gd, int n, const float* pos, const float*
     cudaMemcpyAsync(dIn, pos, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dIn + 3 * R, nrm, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(dIn + 6 * R, wo, 12 * (size_t)n, cudaMemcpyHostToDevice, st);
-    guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, n, rows, gd->bounds, gd->g.scratch.X[0], st);
-    guideInferRows(gd->g, gd->g.scratch.X[0], rows, gd->g.scratch.Y, st);
+    guideFeaturesFromPoints(dIn, dIn + 3 * R, dIn + 6 * R, n, rows, gd->bounds, gd->g.scratch.X0, st);
+    guideInferRows(gd->g, gd->g.scratch.X0, rows, gd->g.scratch.Y, st);
     guideSampleRows(gd->g.scratch.Y, n, seed, dIn + 9 * R, dIn + 12 * R, st);
     cudaMemcpyAsync(dirs, dIn + 9 * R, 12 * (size_t)n, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(pdf, dIn + 12 * R, 4 * (size_t)n, cudaMemcpyDeviceToHost, st);

@@ -71,196 +71,295 @@ __device__ __forceinline__ void warpLayer(const __nv_bfloat16* in, int ldi, cons
 }
 
 // --------------------------------------------------------------- training --
-// Features of training records -> X0 (bf16 [rows][64]); rows >= n are zero.
-__global__ void k_recordFeatures(const GuideRecord* rec, int n, int rowsPad, GuideBounds gb, __nv_bfloat16* X0,
-                                 float4* dirw) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rowsPad) return;
-    __nv_bfloat16* x = X0 + (size_t)r * 64;
-    if (r >= n) {
-        for (int i = 0; i < 64; ++i) x[i] = __float2bfloat16(0.f);
-        dirw[r] = make_float4(0.f, 0.f, 1.f, 0.f);
-        return;
-    }
-    GuideRecord g = rec[r];
-    float p[3] = {(g.p.x - gb.lo[0]) * gb.invExtent[0], (g.p.y - gb.lo[1]) * gb.invExtent[1],
-                  (g.p.z - gb.lo[2]) * gb.invExtent[2]};
-    float nn[3] = {g.n.x, g.n.y, g.n.z}, wo[3] = {g.wo.x, g.wo.y, g.wo.z};
-    for (int i = 0; i < 64; i += 2)
-        *reinterpret_cast<uint32_t*>(x + i) = pack2(guideFeature(i, p, nn, wo), guideFeature(i + 1, p, nn, wo));
-    float w = g.pdf > 0.f ? g.radiance / g.pdf : 0.f;
-    dirw[r] = make_float4(g.wi.x, g.wi.y, g.wi.z, isfinite(w) ? w : 0.f);
+// One Adam step is two launches.
+//   k_trainTiles: a CTA takes 64-row tiles of the batch (4 warps x 16 rows) and
+//     runs the whole step for them out of shared memory -- features, forward
+//     pass, mixture NLL gradient, backward pass, weight and bias gradients -- and
+//     adds the tile's gradients into the CTA's own slot of a partial buffer.
+//   k_reduceAdam: sums the slots of every parameter, normalises by the batch's
+//     total sample weight and takes the Adam step (refreshing the bf16 copies).
+// The loss is -sum_i (w_i / sum_j w_j) log q(wi_i) with w_i = radiance / pdf;
+// rows enter with their raw weight and the slot sums are divided by sum_j w_j,
+// which is the same gradient. Weight gradients dW = dZ^T X are tensor-core
+// products over the tile's rows: both operands are read transposed from
+// shared memory with ldmatrix.trans.
+constexpr int kTileRows = 64;
+constexpr int kLd = 72;   // shared row stride (bf16) of 64-wide rows (144 B: ldmatrix and fragment loads conflict-free)
+constexpr int kLdO = 56;  // shared row stride (bf16) of 48-wide rows (112 B)
+constexpr int kSlot = kGuideParams + 4;  // partial gradient of one CTA, then its weight sum and loss sum
+constexpr int kMaxSlots = 256;
+
+struct TrainSmem {
+    __nv_bfloat16 W[3][64 * kLd];  // [out][in]
+    __nv_bfloat16 W3[kGuideOutPad * kLd];
+    __nv_bfloat16 WT[3][64 * kLd];  // [in][out]
+    __nv_bfloat16 WT3[64 * kLdO];
+    float bias[4][64];
+    __nv_bfloat16 X[4][kTileRows * kLd];  // layer inputs
+    __nv_bfloat16 dY[kTileRows * kLdO];   // output-layer gradient
+    __nv_bfloat16 dZ[3][kTileRows * kLd];  // hidden pre-activation gradients (layers 0..2)
+    float Y[kTileRows * kGuideOutPad];
+    float4 dirw[kTileRows];
+    float red[2][4];
+};
+
+__device__ __forceinline__ uint32_t smemAddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldsmX4T(uint32_t (&r)[4], const __nv_bfloat16* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smemAddr(p)));
 }
 
-// One layer over all rows: warps take 16-row slabs.
+// out[16][N] = act(in[16][64] . W^T + b) for the warp's 16 rows; W [N][64] with row stride ldw.
 template <int N, bool RELU, bool OUT_F32>
-__global__ void k_layerForward(const __nv_bfloat16* X, const __nv_bfloat16* W, const float* bias, int rows,
-                               __nv_bfloat16* Yb, float* Yf) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int slabs = rows / 16;
-    if (warp >= slabs) return;
-    const size_t r0 = (size_t)warp * 16;
-    warpLayer<N, RELU, OUT_F32>(X + r0 * 64, 64, W, bias, OUT_F32 ? nullptr : Yb + r0 * 64, 64,
-                                OUT_F32 ? Yf + r0 * kGuideOutPad : nullptr, kGuideOutPad);
-}
-
-__global__ void k_weightSum(const float4* dirw, int n, float* sum) {
-    float s = 0.f;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) s += dirw[r].w;
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sum, s);
-}
-
-// Output-layer gradient of the normalised NLL: dY = d/dy [ -(w / mean w) log q ] / n.
-__global__ void k_lossGrad(const float* Y, const float4* dirw, int n, int rowsPad, const float* wsum, __nv_bfloat16* dY,
-                           float* lossSum) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    float loss = 0.f;
-    if (r < rowsPad) {
-        __nv_bfloat16* d = dY + (size_t)r * kGuideOutPad;
-        if (r < n && *wsum > 0.f) {
-            float4 dw = dirw[r];
-            float w = dw.w / *wsum;  // weights normalised to sum to one over the batch
-            float dy[kGuideOut];
-            loss = mixtureNllGrad(Y + (size_t)r * kGuideOutPad, V3(dw.x, dw.y, dw.z), w, dy);
-            for (int i = 0; i < kGuideOut; i += 2) *reinterpret_cast<uint32_t*>(d + i) = pack2(dy[i], dy[i + 1]);
-        } else {
-            for (int i = 0; i < kGuideOut; i += 2) *reinterpret_cast<uint32_t*>(d + i) = 0u;
-        }
-        for (int i = kGuideOut; i < kGuideOutPad; i += 2) *reinterpret_cast<uint32_t*>(d + i) = 0u;
-    }
-    for (int off = 16; off > 0; off >>= 1) loss += __shfl_down_sync(0xFFFFFFFFu, loss, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(lossSum, loss);
-}
-
-// dX[r][i] = (sum_o dY[r][o] W[o][i]) * (Xact[r][i] > 0), K = KO (48 or 64); WT = W^T [64][KO].
-template <int KO>
-__global__ void k_layerBackwardData(const __nv_bfloat16* dY, const __nv_bfloat16* WT, const __nv_bfloat16* Xact,
-                                    int rows, __nv_bfloat16* dX) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= rows / 16) return;
+__device__ __forceinline__ void warpLayerS(const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
+                                           __nv_bfloat16* outb, float* outf) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const size_t r0 = (size_t)warp * 16;
-    const __nv_bfloat16* in = dY + r0 * KO;
+    uint32_t a[4][4];
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+        a[ks][0] = ld32(in + g * kLd + ks * 16 + 2 * t);
+        a[ks][1] = ld32(in + (g + 8) * kLd + ks * 16 + 2 * t);
+        a[ks][2] = ld32(in + g * kLd + ks * 16 + 2 * t + 8);
+        a[ks][3] = ld32(in + (g + 8) * kLd + ks * 16 + 2 * t + 8);
+    }
+#pragma unroll
+    for (int nt = 0; nt < N / 8; ++nt) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        const __nv_bfloat16* wr = W + (nt * 8 + g) * kLd;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) mma16816(c, a[ks], ld32(wr + ks * 16 + 2 * t), ld32(wr + ks * 16 + 2 * t + 8));
+        const int col = nt * 8 + 2 * t;
+        float v0 = c[0] + bias[col], v1 = c[1] + bias[col + 1], v2 = c[2] + bias[col], v3 = c[3] + bias[col + 1];
+        if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f); }
+        if (OUT_F32) {
+            outf[g * kGuideOutPad + col] = v0; outf[g * kGuideOutPad + col + 1] = v1;
+            outf[(g + 8) * kGuideOutPad + col] = v2; outf[(g + 8) * kGuideOutPad + col + 1] = v3;
+        } else {
+            *reinterpret_cast<uint32_t*>(outb + g * kLd + col) = pack2(v0, v1);
+            *reinterpret_cast<uint32_t*>(outb + (g + 8) * kLd + col) = pack2(v2, v3);
+        }
+    }
+}
+
+// dX[16][64] = (dZ[16][KO] . W) * (Xact > 0) for the warp's 16 rows; WT = W^T [64][KO] with row stride ldwt.
+template <int KO>
+__device__ __forceinline__ void warpBackData(const __nv_bfloat16* dZ, int ldz, const __nv_bfloat16* WT, int ldwt,
+                                             const __nv_bfloat16* Xact, __nv_bfloat16* dX) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     uint32_t a[KO / 16][4];
 #pragma unroll
     for (int ks = 0; ks < KO / 16; ++ks) {
-        a[ks][0] = ld32(in + g * KO + ks * 16 + 2 * t);
-        a[ks][1] = ld32(in + (g + 8) * KO + ks * 16 + 2 * t);
-        a[ks][2] = ld32(in + g * KO + ks * 16 + 2 * t + 8);
-        a[ks][3] = ld32(in + (g + 8) * KO + ks * 16 + 2 * t + 8);
+        a[ks][0] = ld32(dZ + g * ldz + ks * 16 + 2 * t);
+        a[ks][1] = ld32(dZ + (g + 8) * ldz + ks * 16 + 2 * t);
+        a[ks][2] = ld32(dZ + g * ldz + ks * 16 + 2 * t + 8);
+        a[ks][3] = ld32(dZ + (g + 8) * ldz + ks * 16 + 2 * t + 8);
     }
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         float c[4] = {0.f, 0.f, 0.f, 0.f};
-        const __nv_bfloat16* wr = WT + (nt * 8 + g) * KO;
+        const __nv_bfloat16* wr = WT + (nt * 8 + g) * ldwt;
 #pragma unroll
         for (int ks = 0; ks < KO / 16; ++ks) mma16816(c, a[ks], ld32(wr + ks * 16 + 2 * t), ld32(wr + ks * 16 + 2 * t + 8));
         const int col = nt * 8 + 2 * t;
-        const __nv_bfloat16* xr0 = Xact + (r0 + g) * 64 + col;
-        const __nv_bfloat16* xr1 = Xact + (r0 + g + 8) * 64 + col;
-        float m0 = __bfloat162float(xr0[0]) > 0.f, m1 = __bfloat162float(xr0[1]) > 0.f;
-        float m2 = __bfloat162float(xr1[0]) > 0.f, m3 = __bfloat162float(xr1[1]) > 0.f;
-        *reinterpret_cast<uint32_t*>(dX + (r0 + g) * 64 + col) = pack2(c[0] * m0, c[1] * m1);
-        *reinterpret_cast<uint32_t*>(dX + (r0 + g + 8) * 64 + col) = pack2(c[2] * m2, c[3] * m3);
+        const __nv_bfloat16* x0 = Xact + g * kLd + col;
+        const __nv_bfloat16* x1 = Xact + (g + 8) * kLd + col;
+        const float m0 = __bfloat162float(x0[0]) > 0.f, m1 = __bfloat162float(x0[1]) > 0.f;
+        const float m2 = __bfloat162float(x1[0]) > 0.f, m3 = __bfloat162float(x1[1]) > 0.f;
+        *reinterpret_cast<uint32_t*>(dX + g * kLd + col) = pack2(c[0] * m0, c[1] * m1);
+        *reinterpret_cast<uint32_t*>(dX + (g + 8) * kLd + col) = pack2(c[2] * m2, c[3] * m3);
     }
 }
 
-// dW[o][i] += sum_r dY[r][o] X[r][i], db[o] += sum_r dY[r][o]; NO = 48 or 64 output rows.
-// A block takes a chunk of rows; each 16-row slab is staged transposed in shared memory.
-constexpr int kWgRowsPerBlock = 512;
-constexpr int kPadT = 18;  // shared row stride (bf16) of the transposed slabs
-
-template <int NO>
-__global__ void __launch_bounds__(128) k_layerBackwardWeight(const __nv_bfloat16* dY, const __nv_bfloat16* X, int rows,
-                                                             float* dW, float* db) {
-    __shared__ __align__(16) __nv_bfloat16 sY[NO * kPadT];
-    __shared__ __align__(16) __nv_bfloat16 sX[64 * kPadT];
-    __shared__ float sdb[NO];
+// slot[wOff + o * 64 + i] (+)= sum over the tile's 64 rows of D[r][o] X[r][i], o < oValid.
+// Work unit = one 16-row block of o times two 8-column blocks of i; D rows have stride ldd.
+template <int O>
+__device__ __forceinline__ void tileWeightGrad(const __nv_bfloat16* D, int ldd, const __nv_bfloat16* X, float* slot,
+                                               int wOff, int oValid, bool first) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    constexpr int TILES = (NO / 16) * 8;
-    constexpr int PER_WARP = TILES / 4;
-    float acc[PER_WARP][4];
+    const int q = lane >> 3, i8 = lane & 7;
+    for (int u = warp; u < (O / 16) * 4; u += 4) {
+        const int o0 = (u >> 2) * 16, c0 = (u & 3) * 16;
+        float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
-    for (int k = 0; k < PER_WARP; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.f;
-    if (threadIdx.x < NO) sdb[threadIdx.x] = 0.f;
-    const int rBegin = blockIdx.x * kWgRowsPerBlock;
-    const int rEnd = min(rows, rBegin + kWgRowsPerBlock);
-    for (int r0 = rBegin; r0 < rEnd; r0 += 16) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < 16 * NO; e += 128) {
-            int r = e / NO, o = e % NO;
-            sY[o * kPadT + r] = dY[(size_t)(r0 + r) * NO + o];
-        }
-        for (int e = threadIdx.x; e < 16 * 64; e += 128) {
-            int r = e >> 6, i = e & 63;
-            sX[i * kPadT + r] = X[(size_t)(r0 + r) * 64 + i];
-        }
-        __syncthreads();
-        if (threadIdx.x < NO) {
-            float s = 0.f;
-            for (int r = 0; r < 16; ++r) s += __bfloat162float(sY[threadIdx.x * kPadT + r]);
-            sdb[threadIdx.x] += s;
+        for (int ks = 0; ks < kTileRows / 16; ++ks) {
+            const int r0 = ks * 16;
+            uint32_t a[4], b[4];
+            // A = D^T (16 o x 16 r): matrices (r, o), (r, o + 8), (r + 8, o), (r + 8, o + 8)
+            ldsmX4T(a, D + (r0 + i8 + ((q >> 1) << 3)) * ldd + o0 + ((q & 1) << 3));
+            // B = X (16 r x 8 i), two i blocks: matrices (r, i), (r + 8, i), (r, i + 8), (r + 8, i + 8)
+            ldsmX4T(b, X + (r0 + i8 + ((q & 1) << 3)) * kLd + c0 + ((q >> 1) << 3));
+            mma16816(acc[0], a, b[0], b[1]);
+            mma16816(acc[1], a, b[2], b[3]);
         }
 #pragma unroll
-        for (int k = 0; k < PER_WARP; ++k) {
-            const int tile = warp * PER_WARP + k;
-            const int mt = tile / 8, nt = tile % 8;
-            uint32_t a[4];
-            const __nv_bfloat16* ar = sY + (mt * 16) * kPadT;
-            a[0] = ld32(ar + g * kPadT + 2 * t);
-            a[1] = ld32(ar + (g + 8) * kPadT + 2 * t);
-            a[2] = ld32(ar + g * kPadT + 2 * t + 8);
-            a[3] = ld32(ar + (g + 8) * kPadT + 2 * t + 8);
-            const __nv_bfloat16* br = sX + (nt * 8 + g) * kPadT;
-            mma16816(acc[k], a, ld32(br + 2 * t), ld32(br + 2 * t + 8));
+        for (int h = 0; h < 2; ++h) {
+            const int i = c0 + h * 8 + 2 * t;
+            const int oa = o0 + g, ob = o0 + g + 8;
+            float* pa = slot + wOff + oa * 64 + i;
+            float* pb = slot + wOff + ob * 64 + i;
+            if (oa < oValid) {
+                if (first) { pa[0] = acc[h][0]; pa[1] = acc[h][1]; } else { pa[0] += acc[h][0]; pa[1] += acc[h][1]; }
+            }
+            if (ob < oValid) {
+                if (first) { pb[0] = acc[h][2]; pb[1] = acc[h][3]; } else { pb[0] += acc[h][2]; pb[1] += acc[h][3]; }
+            }
         }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_trainTiles(const GuideRecord* rec, int n, int tiles, GuideBounds gb,
+                                                    GuideWeights w, float* partial) {
+    extern __shared__ __align__(128) unsigned char smemRaw[];
+    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smemRaw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights and biases, once per CTA (rows of 128 B as 16-byte pieces)
+    for (int e = tid; e < 3 * 64 * 8; e += 128) {
+        const int l = e / 512, r = (e >> 3) & 63, c = e & 7;
+        *reinterpret_cast<uint4*>(S.W[l] + r * kLd + 8 * c) = reinterpret_cast<const uint4*>(w.W[l] + r * 64)[c];
+        *reinterpret_cast<uint4*>(S.WT[l] + r * kLd + 8 * c) = reinterpret_cast<const uint4*>(w.WT[l] + r * 64)[c];
+    }
+    for (int e = tid; e < kGuideOutPad * 8; e += 128) {
+        const int r = e >> 3, c = e & 7;
+        *reinterpret_cast<uint4*>(S.W3 + r * kLd + 8 * c) = reinterpret_cast<const uint4*>(w.W[3] + r * 64)[c];
+    }
+    for (int e = tid; e < 64 * 6; e += 128) {
+        const int r = e / 6, c = e % 6;
+        *reinterpret_cast<uint4*>(S.WT3 + r * kLdO + 8 * c) =
+            reinterpret_cast<const uint4*>(w.WT[3] + r * kGuideOutPad)[c];
+    }
+    for (int e = tid; e < 4 * 64; e += 128) {
+        const int l = e >> 6, o = e & 63;
+        S.bias[l][o] = (l < 3 || o < kGuideOutPad) ? w.bias[l][o] : 0.f;
+    }
+    float* slot = partial + (size_t)blockIdx.x * kSlot;
+    float wsum = 0.f, lsum = 0.f;
+    bool first = true;
+    const int r0 = warp * 16;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, first = false) {
+        __syncthreads();  // weights staged / the previous tile's shared data consumed
+        {   // features: two threads per row, 32 features each
+            const int r = tid >> 1, half = tid & 1;
+            const int gr = tile * kTileRows + r;
+            __nv_bfloat16* x = S.X[0] + r * kLd + half * 32;
+            if (gr < n) {
+                const GuideRecord& gd = rec[gr];
+                const float p[3] = {(gd.p.x - gb.lo[0]) * gb.invExtent[0], (gd.p.y - gb.lo[1]) * gb.invExtent[1],
+                                    (gd.p.z - gb.lo[2]) * gb.invExtent[2]};
+                const float nn[3] = {gd.n.x, gd.n.y, gd.n.z}, wo[3] = {gd.wo.x, gd.wo.y, gd.wo.z};
+#pragma unroll 4
+                for (int i = 0; i < 32; i += 2)
+                    *reinterpret_cast<uint32_t*>(x + i) =
+                        pack2(guideFeature(half * 32 + i, p, nn, wo), guideFeature(half * 32 + i + 1, p, nn, wo));
+                if (half == 0) {
+                    const float wgt = gd.pdf > 0.f ? gd.radiance / gd.pdf : 0.f;
+                    S.dirw[r] = make_float4(gd.wi.x, gd.wi.y, gd.wi.z, isfinite(wgt) ? wgt : 0.f);
+                }
+            } else {
+                for (int i = 0; i < 32; i += 2) *reinterpret_cast<uint32_t*>(x + i) = 0u;
+                if (half == 0) S.dirw[r] = make_float4(0.f, 0.f, 1.f, 0.f);
+            }
+        }
+        __syncthreads();
+        // forward, each warp on its 16 rows
+        warpLayerS<64, true, false>(S.X[0] + r0 * kLd, S.W[0], S.bias[0], S.X[1] + r0 * kLd, nullptr);
+        __syncwarp();
+        warpLayerS<64, true, false>(S.X[1] + r0 * kLd, S.W[1], S.bias[1], S.X[2] + r0 * kLd, nullptr);
+        __syncwarp();
+        warpLayerS<64, true, false>(S.X[2] + r0 * kLd, S.W[2], S.bias[2], S.X[3] + r0 * kLd, nullptr);
+        __syncwarp();
+        warpLayerS<kGuideOutPad, false, true>(S.X[3] + r0 * kLd, S.W3, S.bias[3], nullptr, S.Y + r0 * kGuideOutPad);
+        __syncwarp();
+        // output gradient of -w log q, one lane per row
+        if (lane < 16) {
+            const int r = r0 + lane;
+            __nv_bfloat16* d = S.dY + r * kLdO;
+            const float4 dw = S.dirw[r];
+            if (dw.w > 0.f) {
+                float dy[kGuideOut];
+                lsum += mixtureNllGrad(S.Y + r * kGuideOutPad, V3(dw.x, dw.y, dw.z), dw.w, dy);
+                wsum += dw.w;
+                for (int i = 0; i < kGuideOut; i += 2) *reinterpret_cast<uint32_t*>(d + i) = pack2(dy[i], dy[i + 1]);
+            } else {
+                for (int i = 0; i < kGuideOut; i += 2) *reinterpret_cast<uint32_t*>(d + i) = 0u;
+            }
+            for (int i = kGuideOut; i < kGuideOutPad; i += 2) *reinterpret_cast<uint32_t*>(d + i) = 0u;
+        }
+        __syncwarp();
+        // backward through the hidden layers
+        warpBackData<kGuideOutPad>(S.dY + r0 * kLdO, kLdO, S.WT3, kLdO, S.X[3] + r0 * kLd, S.dZ[2] + r0 * kLd);
+        __syncwarp();
+        warpBackData<64>(S.dZ[2] + r0 * kLd, kLd, S.WT[2], kLd, S.X[2] + r0 * kLd, S.dZ[1] + r0 * kLd);
+        __syncwarp();
+        warpBackData<64>(S.dZ[1] + r0 * kLd, kLd, S.WT[1], kLd, S.X[1] + r0 * kLd, S.dZ[0] + r0 * kLd);
+        __syncthreads();
+        // weight gradients over all 64 rows of the tile
+        tileWeightGrad<64>(S.dZ[0], kLd, S.X[0], slot, kGuideW0, 64, first);
+        tileWeightGrad<64>(S.dZ[1], kLd, S.X[1], slot, kGuideW1, 64, first);
+        tileWeightGrad<64>(S.dZ[2], kLd, S.X[2], slot, kGuideW2, 64, first);
+        tileWeightGrad<kGuideOutPad>(S.dY, kLdO, S.X[3], slot, kGuideW3, kGuideOut, first);
+        // bias gradients: 64 + 64 + 64 + 40 columns
+        for (int c = tid; c < 192 + kGuideOut; c += 128) {
+            const int l = c < 192 ? c >> 6 : 3, o = c < 192 ? c & 63 : c - 192;
+            const __nv_bfloat16* D = l < 3 ? S.dZ[l] : S.dY;
+            const int ld = l < 3 ? kLd : kLdO;
+            float sum = 0.f;
+            for (int r = 0; r < kTileRows; ++r) sum += __bfloat162float(D[r * ld + o]);
+            const int off = (l == 0 ? kGuideB0 : l == 1 ? kGuideB1 : l == 2 ? kGuideB2 : kGuideB3) + o;
+            slot[off] = first ? sum : slot[off] + sum;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        wsum += __shfl_down_sync(0xFFFFFFFFu, wsum, off);
+        lsum += __shfl_down_sync(0xFFFFFFFFu, lsum, off);
+    }
+    if (lane == 0) { S.red[0][warp] = wsum; S.red[1][warp] = lsum; }
+    __syncthreads();
+    if (tid == 0) {
+        slot[kGuideParams] = (S.red[0][0] + S.red[0][1]) + (S.red[0][2] + S.red[0][3]);
+        slot[kGuideParams + 1] = (S.red[1][0] + S.red[1][1]) + (S.red[1][2] + S.red[1][3]);
+    }
+}
+
+// Gradient = slot sum / total weight; Adam (lr > 0) on the fp32 master
+// parameters with bias corrections c1, c2, refreshing the bf16 copies.
+// scalars[0] = total weight, scalars[1] = loss.
+__global__ void k_reduceAdam(const float* partial, int slots, float* grads, float* params, float* m, float* v,
+                             float lr, float b1, float b2, float eps, float c1, float c2, GuideWeights w,
+                             float* scalars) {
+    __shared__ float tot[2];
+    if (threadIdx.x < 32) {
+        float ws = 0.f, ls = 0.f;
+        for (int s = threadIdx.x; s < slots; s += 32) {
+            ws += partial[(size_t)s * kSlot + kGuideParams];
+            ls += partial[(size_t)s * kSlot + kGuideParams + 1];
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            ws += __shfl_down_sync(0xFFFFFFFFu, ws, off);
+            ls += __shfl_down_sync(0xFFFFFFFFu, ls, off);
+        }
+        if (threadIdx.x == 0) { tot[0] = ws; tot[1] = ls; }
     }
     __syncthreads();
-#pragma unroll
-    for (int k = 0; k < PER_WARP; ++k) {
-        const int tile = warp * PER_WARP + k;
-        const int mt = tile / 8, nt = tile % 8;
-        const int o0 = mt * 16 + g, i0 = nt * 8 + 2 * t;
-        atomicAdd(&dW[o0 * 64 + i0], acc[k][0]);
-        atomicAdd(&dW[o0 * 64 + i0 + 1], acc[k][1]);
-        atomicAdd(&dW[(o0 + 8) * 64 + i0], acc[k][2]);
-        atomicAdd(&dW[(o0 + 8) * 64 + i0 + 1], acc[k][3]);
-    }
-    if (threadIdx.x < NO) atomicAdd(&db[threadIdx.x], sdb[threadIdx.x]);
-}
-
-// Adam on the fp32 master parameters; refreshes the bf16 copies W / WT.
-__global__ void k_adam(float* params, const float* grads, float* m, float* v, int n, float lr, float b1, float b2,
-                       float eps, float c1, float c2, GuideWeights w) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float g = grads[i];
-    float mi = b1 * m[i] + (1.f - b1) * g;
-    float vi = b2 * v[i] + (1.f - b2) * g * g;
-    m[i] = mi;
-    v[i] = vi;
-    float p = params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    params[i] = p;
-    guideStoreBf16(w, i, p);
-}
-
-// Gradient layout follows the parameters: dW rows are 64 wide; the last layer's
-// gradient rows 40..47 (padding) are dropped when copied into the flat vector.
-__global__ void k_gatherGrads(const float* dW0, const float* dW1, const float* dW2, const float* dW3, const float* db,
-                              float* grads) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float W = tot[0];
+    const float inv = W > 0.f ? 1.f / W : 0.f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) { scalars[0] = W; scalars[1] = tot[1] * inv; }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kGuideParams) return;
-    float v;
-    if (i < kGuideB0) v = dW0[i - kGuideW0];
-    else if (i < kGuideW1) v = db[i - kGuideB0];
-    else if (i < kGuideB1) v = dW1[i - kGuideW1];
-    else if (i < kGuideW2) v = db[64 + i - kGuideB1];
-    else if (i < kGuideB2) v = dW2[i - kGuideW2];
-    else if (i < kGuideW3) v = db[128 + i - kGuideB2];
-    else if (i < kGuideB3) v = dW3[i - kGuideW3];
-    else v = db[192 + i - kGuideB3];
-    grads[i] = v;
+    float sum = 0.f;
+    for (int s = 0; s < slots; ++s) sum += partial[(size_t)s * kSlot + i];
+    const float gr = sum * inv;
+    grads[i] = gr;
+    if (lr > 0.f) {
+        const float mi = b1 * m[i] + (1.f - b1) * gr;
+        const float vi = b2 * v[i] + (1.f - b2) * gr * gr;
+        m[i] = mi;
+        v[i] = vi;
+        const float p = params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        params[i] = p;
+        guideStoreBf16(w, i, p);
+    }
 }
 
 }  // namespace
@@ -328,40 +427,22 @@ void guideInferRows(const GuideDevice& g, const __nv_bfloat16* X0, int rowsPad, 
 void guideTrainStep(GuideDevice& g, const GuideRecord* rec, int n, GuideBounds gb, float lr, cudaStream_t s) {
     n = std::min(n, g.maxRows);
     if (n <= 0) return;
-    const int rows = (n + 63) & ~63;
-    GuideScratch sc = g.scratch;
-    k_recordFeatures<<<(rows + 127) / 128, 128, 0, s>>>(rec, n, rows, gb, sc.X[0], sc.dirw);
-    const int wb = (rows / 16 + 3) / 4;
-    k_layerForward<64, true, false><<<wb, 128, 0, s>>>(sc.X[0], g.w.W[0], g.w.bias[0], rows, sc.X[1], nullptr);
-    k_layerForward<64, true, false><<<wb, 128, 0, s>>>(sc.X[1], g.w.W[1], g.w.bias[1], rows, sc.X[2], nullptr);
-    k_layerForward<64, true, false><<<wb, 128, 0, s>>>(sc.X[2], g.w.W[2], g.w.bias[2], rows, sc.X[3], nullptr);
-    k_layerForward<kGuideOutPad, false, true><<<wb, 128, 0, s>>>(sc.X[3], g.w.W[3], g.w.bias[3], rows, nullptr, sc.Y);
-    cudaMemsetAsync(sc.scalars, 0, 4 * sizeof(float), s);
-    k_weightSum<<<std::min(64, (rows + 255) / 256), 256, 0, s>>>(sc.dirw, rows, sc.scalars);
-    k_lossGrad<<<(rows + 127) / 128, 128, 0, s>>>(sc.Y, sc.dirw, n, rows, sc.scalars, sc.dY3, sc.scalars + 1);
-    k_layerBackwardData<kGuideOutPad><<<wb, 128, 0, s>>>(sc.dY3, g.w.WT[3], sc.X[3], rows, sc.dZ[2]);
-    k_layerBackwardData<64><<<wb, 128, 0, s>>>(sc.dZ[2], g.w.WT[2], sc.X[2], rows, sc.dZ[1]);
-    k_layerBackwardData<64><<<wb, 128, 0, s>>>(sc.dZ[1], g.w.WT[1], sc.X[1], rows, sc.dZ[0]);
-    cudaMemsetAsync(sc.dW, 0, sizeof(float) * (3 * 64 * 64 + kGuideOutPad * 64 + 256), s);
-    const int gw = (rows + kWgRowsPerBlock - 1) / kWgRowsPerBlock;
-    float* dW0 = sc.dW;
-    float* dW1 = dW0 + 64 * 64;
-    float* dW2 = dW1 + 64 * 64;
-    float* dW3 = dW2 + 64 * 64;
-    float* db = dW3 + kGuideOutPad * 64;
-    k_layerBackwardWeight<64><<<gw, 128, 0, s>>>(sc.dZ[0], sc.X[0], rows, dW0, db);
-    k_layerBackwardWeight<64><<<gw, 128, 0, s>>>(sc.dZ[1], sc.X[1], rows, dW1, db + 64);
-    k_layerBackwardWeight<64><<<gw, 128, 0, s>>>(sc.dZ[2], sc.X[2], rows, dW2, db + 128);
-    k_layerBackwardWeight<kGuideOutPad><<<gw, 128, 0, s>>>(sc.dY3, sc.X[3], rows, dW3, db + 192);
-    k_gatherGrads<<<(kGuideParams + 255) / 256, 256, 0, s>>>(dW0, dW1, dW2, dW3, db, g.grads);
+    const int tiles = (n + kTileRows - 1) / kTileRows;
+    const int slots = std::min(tiles, kMaxSlots);
+    cudaFuncSetAttribute(k_trainTiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem));
+    k_trainTiles<<<slots, 128, sizeof(TrainSmem), s>>>(rec, n, tiles, gb, g.w, g.scratch.partial);
+    const float b1 = 0.9f, b2 = 0.999f;
+    float c1 = 1.f, c2 = 1.f;
     if (lr > 0.f) {
         g.step += 1;
-        const float b1 = 0.9f, b2 = 0.999f;
-        float c1 = 1.f - std::pow(b1, (float)g.step), c2 = 1.f - std::pow(b2, (float)g.step);
-        k_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g.params, g.grads, g.m, g.v, kGuideParams, lr, b1, b2, 1e-8f,
-                                                         c1, c2, g.w);
+        c1 = 1.f - std::pow(b1, (float)g.step);
+        c2 = 1.f - std::pow(b2, (float)g.step);
     }
+    k_reduceAdam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g.scratch.partial, slots, g.grads, g.params, g.m, g.v, lr,
+                                                            b1, b2, 1e-8f, c1, c2, g.w, g.scratch.scalars);
 }
+
+size_t guidePartialBytes() { return sizeof(float) * (size_t)kSlot * kMaxSlots; }
 
 namespace {
 // Credited wavefront records -> training pool; records that carry no radiance

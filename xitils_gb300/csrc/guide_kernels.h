@@ -19,13 +19,10 @@ struct GuideWeights {
 };
 
 struct GuideScratch {
-    __nv_bfloat16* X[4];   // layer inputs [rows][64]
-    float4* dirw;          // wi and sample weight per row
-    float* Y;              // outputs [rows][48]
-    __nv_bfloat16* dY3;    // output gradient [rows][48]
-    __nv_bfloat16* dZ[3];  // hidden gradients [rows][64]
-    float* dW;             // 3 x 64x64 + 48x64 weight gradients, then 256 bias gradients
-    float* scalars;        // [0] weight sum, [1] loss sum
+    __nv_bfloat16* X0;  // feature rows [rows][64] of the inference entry points
+    float* Y;           // outputs [rows][48]
+    float* partial;     // per-CTA partial gradients of a training step (guidePartialBytes())
+    float* scalars;     // [0] total sample weight, [1] loss of the last training step
 };
 
 struct GuideDevice {
@@ -48,6 +45,8 @@ __device__ void guideStoreBf16(const GuideWeights& w, int i, float p);
 
 void guideRefresh(const GuideDevice& g, cudaStream_t s);
 void guideInferRows(const GuideDevice& g, const __nv_bfloat16* X0, int rowsPad, float* Y, cudaStream_t s);
+// Bytes of GuideScratch::partial.
+size_t guidePartialBytes();
 // One Adam step (lr > 0) or gradients only (lr == 0) on records [0, n) (at most maxRows).
 void guideTrainStep(GuideDevice& g, const GuideRecord* rec, int n, GuideBounds gb, float lr, cudaStream_t s);
 // Training targets of the records [0, min(*nDev, cap)) from the per-path accumulators.

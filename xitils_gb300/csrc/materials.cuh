@@ -42,6 +42,31 @@ __device__ __forceinline__ V3 texLookup(const TextureDev& t, float u, float v) {
     return texAt(t, (int)(u * (float)t.w), (int)(v * (float)t.h));
 }
 
+// Texture::rgbDifferentialU / V (Texture.h:105-155): central differences of a
+// texel, ((rgb(x + 1, y) - rgb(x - 1, y)) / 2) * width, bilinearly weighted like
+// rgb(uv). The U derivative addresses rows from 1 - v, the V derivative from v,
+// as the reference does (only the red channel is returned).
+__device__ __forceinline__ float texDiffUAt(const TextureDev& t, int x, int y) {
+    return ((texAt(t, x + 1, y).x - texAt(t, x - 1, y).x) * 0.5f) * (float)t.w;
+}
+__device__ __forceinline__ float texDiffVAt(const TextureDev& t, int x, int y) {
+    return ((texAt(t, x, y + 1).x - texAt(t, x, y - 1).x) * 0.5f) * (float)t.h;
+}
+template <bool U>
+__device__ __forceinline__ float texDiff(const TextureDev& t, float u, float v) {
+    const float vv = U ? 1.0f - v : v;
+    auto at = [&](int x, int y) { return U ? texDiffUAt(t, x, y) : texDiffVAt(t, x, y); };
+    if (t.filter) {
+        float fx = u * (float)t.w - 0.5f, fy = vv * (float)t.h - 0.5f;
+        int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+        float wx1 = fx - (float)x0, wy1 = fy - (float)y0;
+        float wx0 = 1.0f - wx1, wy0 = 1.0f - wy1;
+        return (wx0 * wy0) * at(x0, y0) + (wx0 * wy1) * at(x0, y0 + 1) + (wx1 * wy0) * at(x0 + 1, y0) +
+               (wx1 * wy1) * at(x0 + 1, y0 + 1);
+    }
+    return at((int)(u * (float)t.w), (int)(vv * (float)t.h));
+}
+
 // ------------------------------------------------------------------- skies --
 __device__ __forceinline__ V3 skyRadiance(const SceneDev& sc, V3 wi) {
     switch (sc.skyKind) {
@@ -433,6 +458,14 @@ __device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instanc
         s.sbit = V3();
     }
     s.sn = faceForward(s.sn, s.wo);
+    if (m.shellLayers) {  // TriangleIndexedWithShellMapping::perturbIntersection (TriangleIndexed.h:237-254)
+        const TextureDev d{m.shellTexels, m.shellW, m.shellH, m.shellClamp, m.shellFilter};
+        V3 a(-texDiff<true>(d, s.uv.x, s.uv.y) * m.shellScale, -texDiff<false>(d, s.uv.x, s.uv.y) * m.shellScale, 1.0f);
+        a = normalize(a);
+        s.sn = normalize(a.x * s.stan + a.y * s.sbit + a.z * s.sn);
+        s.stan = V3();
+        s.sbit = V3();
+    }
     // object -> world (an identity matrix product is exact, its normalize is not skipped)
     if (!in.identity) s.p = xformPoint(in.mat, s.p);
     s.n = in.identity ? normalize(s.n) : xformNormal(in.mat, s.n);

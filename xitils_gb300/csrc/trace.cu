@@ -707,14 +707,16 @@ static int persistentGrid(K kernel, int numSMs) {
     return numSMs * it->second;
 }
 
+// The specialised kernels (one instance, flat instance lists, wide BVHs) have no
+// shell-mapping discard; a scene with a shell-mapped mesh takes the generic pair.
 void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, bool count, cudaStream_t s) {
     RenderParams none{};
-    const bool flat = sc.nInstances <= kFlatInstances;
+    const bool flat = sc.nInstances <= kFlatInstances && !sc.shell;
 #define XGB_LAUNCH(K) K<<<persistentGrid(K, numSMs), kTraceBlock, 0, s>>>
     if (flat && sc.blasLayout == 1) {
         if (count) XGB_LAUNCH((k_trace_wide<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_wide<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-    } else if (sc.nInstances == 1 && sc.blasLayout == 0) {
+    } else if (sc.nInstances == 1 && sc.blasLayout == 0 && !sc.shell) {
         if (count) XGB_LAUNCH((k_trace_single<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_single<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (flat && sc.blasLayout == 0) {
@@ -737,9 +739,9 @@ void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* 
 
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s) {
-    const bool flat = sc.nInstances <= kFlatInstances;
+    const bool flat = sc.nInstances <= kFlatInstances && !sc.shell;
     if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
-    else if (sc.nInstances == 1 && sc.blasLayout == 0)
+    else if (sc.nInstances == 1 && sc.blasLayout == 0 && !sc.shell)
         XGB_LAUNCH((k_trace_single<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (flat && sc.blasLayout == 0)
         XGB_LAUNCH((k_trace_flat2<true, false, OneScene>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);

@@ -192,6 +192,47 @@ __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r,
     return mask;
 }
 
+// ---- shell mapping ---------------------------------------------------------------
+// Red channel of the displacement texture at (u, v): Texture::rgb(uv) with its
+// clamp / wrap addressing and bilinear or nearest filter (Texture.h:83-103,
+// :161-171), in explicitly unfused float operations.
+__device__ __forceinline__ float shellTexel(const MeshDev& m, int x, int y) {
+    if (m.shellClamp) {
+        x = x < 0 ? 0 : (x > m.shellW - 1 ? m.shellW - 1 : x);
+        y = y < 0 ? 0 : (y > m.shellH - 1 ? m.shellH - 1 : y);
+    } else {
+        x %= m.shellW; y %= m.shellH;
+        if (x < 0) x += m.shellW;
+        if (y < 0) y += m.shellH;
+    }
+    return __ldg(&m.shellTexels[(size_t)x + (size_t)y * m.shellW]).x;
+}
+__device__ __forceinline__ float shellRed(const MeshDev& m, float u, float v) {
+    const float W = (float)m.shellW, H = (float)m.shellH;
+    if (!m.shellFilter) return shellTexel(m, (int)__fmul_rn(u, W), (int)__fmul_rn(v, H));
+    const float fx = __fsub_rn(__fmul_rn(u, W), 0.5f), fy = __fsub_rn(__fmul_rn(v, H), 0.5f);
+    const int x0 = (int)floorf(fx), y0 = (int)floorf(fy);
+    const float wx1 = __fsub_rn(fx, (float)x0), wy1 = __fsub_rn(fy, (float)y0);
+    const float wx0 = __fsub_rn(1.0f, wx1), wy0 = __fsub_rn(1.0f, wy1);
+    float r = __fmul_rn(__fmul_rn(wx0, wy0), shellTexel(m, x0, y0));
+    r = __fadd_rn(r, __fmul_rn(__fmul_rn(wx0, wy1), shellTexel(m, x0, y0 + 1)));
+    r = __fadd_rn(r, __fmul_rn(__fmul_rn(wx1, wy0), shellTexel(m, x0 + 1, y0)));
+    return __fadd_rn(r, __fmul_rn(__fmul_rn(wx1, wy1), shellTexel(m, x0 + 1, y0 + 1)));
+}
+// TriangleIndexedWithShellMapping::discardByAlpha (TriangleIndexed.h:233-235),
+// asked by TriangleIndexed::intersect once the hit is inside [0, tMax]
+// (:132-141): the texcoord lerp(uv0, uv1, uv2, b0, b1) (Utils.h:81-83), then
+// red < height with height = layer / (layers - 1) (TriangleMesh.h:305-318).
+__device__ __noinline__ bool shellDiscard(const MeshDev& m, int prim, float b0, float b1) {
+    const int i0 = __ldg(&m.idx[3 * prim]), i1 = __ldg(&m.idx[3 * prim + 1]), i2 = __ldg(&m.idx[3 * prim + 2]);
+    const float2 a = __ldg(&m.uv[i0]), b = __ldg(&m.uv[i1]), c = __ldg(&m.uv[i2]);
+    const float w = __fsub_rn(__fsub_rn(1.0f, b0), b1);
+    const float u = __fadd_rn(__fadd_rn(__fmul_rn(a.x, b0), __fmul_rn(b.x, b1)), __fmul_rn(c.x, w));
+    const float v = __fadd_rn(__fadd_rn(__fmul_rn(a.y, b0), __fmul_rn(b.y, b1)), __fmul_rn(c.y, w));
+    const float height = __fdiv_rn((float)(prim / m.shellFaces), (float)(m.shellLayers - 1));
+    return shellRed(m, u, v) < height;
+}
+
 // Watertight tests of `cnt` triangles from `first`; ANY: stops at the first hit.
 template <bool ANY>
 __device__ __forceinline__ bool testTris(const TriV* tris, int first, int cnt, const WRay& r, float& tMax, TraceHit& hit,
@@ -202,6 +243,28 @@ __device__ __forceinline__ bool testTris(const TriV* tris, int first, int cnt, c
         const float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
         float t, b0, b1;
         if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+            tMax = t;
+            found = true;
+            if (ANY) return true;
+            hit.t = t; hit.b0 = b0; hit.b1 = b1;
+            hit.prim = __float_as_int(p0.w);
+            hit.inst = inst;
+        }
+    }
+    return found;
+}
+
+// testTris for a mesh that may be shell-mapped (generic traversal path).
+template <bool ANY>
+__device__ __forceinline__ bool testTrisMesh(const MeshDev& m, int first, int cnt, const WRay& r, float& tMax,
+                                             TraceHit& hit, int inst) {
+    if (!m.shellLayers) return testTris<ANY>(m.tris, first, cnt, r, tMax, hit, inst);
+    bool found = false;
+    for (int k = 0; k < cnt; ++k) {
+        const TriV* tv = m.tris + first + k;
+        const float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
+        float t, b0, b1;
+        if (watertight(r, p0, p1, p2, tMax, t, b0, b1) && !shellDiscard(m, __float_as_int(p0.w), b0, b1)) {
             tMax = t;
             found = true;
             if (ANY) return true;
@@ -253,6 +316,7 @@ __device__ __forceinline__ bool traverseBlas2(const MeshDev& m, const WRay& r, f
                 float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
                 float t, b0, b1;
                 if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+                    if (m.shellLayers && shellDiscard(m, __float_as_int(p0.w), b0, b1)) continue;
                     tMax = t;
                     found = true;
                     if (ANY) return true;
@@ -274,7 +338,7 @@ __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r
                                                  unsigned int* errors, WorkCount& wc) {
     if (m.rootIsLeaf) {
         if (COUNT) wc.tris += m.nTris;
-        return testTris<ANY>(m.tris, 0, m.nTris, r, tMax, hit, inst);
+        return testTrisMesh<ANY>(m, 0, m.nTris, r, tMax, hit, inst);
     }
     const int oct = rayOctant(r);
     unsigned int stack[kWideStack];
@@ -308,7 +372,7 @@ __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r
         } else {
             const int cnt = (int)(mb >> 5);
             if (COUNT) wc.tris += cnt;
-            if (testTris<ANY>(m.tris, h.triBase + (int)(mb & 31u), cnt, r, tMax, hit, inst)) {
+            if (testTrisMesh<ANY>(m, h.triBase + (int)(mb & 31u), cnt, r, tMax, hit, inst)) {
                 found = true;
                 if (ANY) return true;
             }

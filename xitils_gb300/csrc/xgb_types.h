@@ -72,6 +72,14 @@ struct MeshDev {
     int nVerts;
     int rootIsLeaf;  // 1 when the whole mesh is one leaf (no nodes): <= kLeafMax triangles (binary), <= kWideLeafMax (wide)
     int rootLeaf;    // leafEncode(0, nTris) of that leaf
+    // Shell mapping (TriangleIndexedWithShellMapping, TriangleIndexed.h:220-256):
+    // triangle t lies on layer t / shellFaces of shellLayers; shellLayers = 0
+    // for an ordinary mesh.
+    int shellLayers;
+    int shellFaces;
+    float shellScale;
+    const float4* shellTexels;  // displacement texture (red channel used)
+    int shellW, shellH, shellClamp, shellFilter;
 };
 
 struct __align__(16) Instance {
@@ -137,6 +145,7 @@ struct SceneDev {
     int tlasRootIsLeaf;
     int blasLayout;  // every mesh binary (0), every mesh wide (1), or a mix (2)
     int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
+    int shell;       // 1 when some mesh is shell-mapped (its hits can be discarded during traversal)
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;

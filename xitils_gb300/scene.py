@@ -41,10 +41,11 @@ class MeshDesc:
     nrm: Optional[np.ndarray] = None
     tan: Optional[np.ndarray] = None
     bit: Optional[np.ndarray] = None
+    shell: Optional[tuple] = None  # (displacement texture, scale, layers): shell-mapped mesh
 
     @property
     def n_tris(self) -> int:
-        return int(self.idx.size // 3)
+        return int(self.idx.size // 3) * (self.shell[2] if self.shell else 1)
 
 
 @dataclass
@@ -104,6 +105,16 @@ class SceneDesc:
         self.meshes.append(m)
         return len(self.meshes) - 1
 
+    def add_mesh_shell(self, pos, idx, uv, nrm, tan, bit, displacement: int, scale: float, layers: int) -> int:
+        """Shell-mapped mesh (TriangleMesh::setGeometryWithShellMapping): `layers`
+        copies offset along the normals up to `scale`, texture `displacement`'s
+        red channel deciding which copy is hit."""
+        i = self.add_mesh(pos, idx, uv, nrm, tan, bit)
+        m = self.meshes[i]
+        assert all(a is not None for a in (m.uv, m.nrm, m.tan, m.bit)), "shell mapping needs every attribute"
+        m.shell = (int(displacement), float(scale), int(layers))
+        return i
+
     def add_material(self, kind: int, f=(), base: int = -1, tex: int = -1, normalmap: int = -1) -> int:
         self.materials.append(MaterialDesc(kind, [float(x) for x in f], base, tex, normalmap))
         return len(self.materials) - 1
@@ -143,7 +154,10 @@ class SceneDesc:
         """World-space box (lo, hi) of every object's vertices (float64)."""
         lo, hi = np.full(3, np.inf), np.full(3, -np.inf)
         for o in self.objects:
-            p = self.meshes[o.mesh].pos.astype(np.float64)
+            mesh = self.meshes[o.mesh]
+            p = mesh.pos.astype(np.float64)
+            if mesh.shell:  # the top layer too
+                p = np.concatenate([p, p + mesh.shell[1] * mesh.nrm.astype(np.float64)])
             m = np.asarray(o.transform.mat, np.float64).reshape(4, 4)
             w = p @ m[:3, :3].T + m[:3, 3]
             lo, hi = np.minimum(lo, w.min(axis=0)), np.maximum(hi, w.max(axis=0))
@@ -157,7 +171,10 @@ class SceneDesc:
         for t in self.textures:
             backend.add_texture(t.rgb, t.clamp, t.filter)
         for m in self.meshes:
-            backend.add_mesh(m.pos, m.idx, m.uv, m.nrm, m.tan, m.bit)
+            if m.shell:
+                backend.add_mesh_shell(m.pos, m.idx, m.uv, m.nrm, m.tan, m.bit, *m.shell)
+            else:
+                backend.add_mesh(m.pos, m.idx, m.uv, m.nrm, m.tan, m.bit)
         for mt in self.materials:
             backend.add_material(mt.kind, mt.f, mt.base, mt.tex, mt.normalmap)
         for o in self.objects:

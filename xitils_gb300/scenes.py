@@ -421,3 +421,63 @@ def mfnm_at_scale(width: int = 2048, height: int = 2048, spp: int = 256, grid: i
     s.set_camera(look_at((0.5, 0.42, -0.25), (0.5, 0.02, 0.55), (0, 1, 0)), 50.0 * math.pi / 180.0, height / width)
     s.fixes = 2  # samples the normal-mapping walk still turns non-finite (0/0 facet weights) are dropped
     return s
+
+
+# ------------------------------------------------------- shell-mapped fabric --
+def weave_displacement(res: int = 256, threads: int = 8) -> np.ndarray:
+    """Plain-weave height map [res, res, 3] in [0, 1]: warp threads along v and
+    weft threads along u with round cross-sections, each passing over and under
+    the crossing threads in turn (r = g = b = height)."""
+    x = (np.arange(res, dtype=np.float64) + 0.5) / res * threads
+    X, Y = np.meshgrid(x, x)  # X follows u (columns), Y follows v (rows)
+    cx = np.abs(np.mod(X, 1.0) - 0.5) * 2.0
+    cy = np.abs(np.mod(Y, 1.0) - 0.5) * 2.0
+    warp = np.sqrt(np.clip(1.0 - cx * cx, 0.0, 1.0)) * (0.55 + 0.45 * np.sin(np.pi * (Y + np.floor(X))))
+    weft = np.sqrt(np.clip(1.0 - cy * cy, 0.0, 1.0)) * (0.55 - 0.45 * np.sin(np.pi * (X + np.floor(Y))))
+    h = np.clip(np.maximum(warp, weft), 0.0, 1.0)
+    return np.repeat(h[..., None], 3, axis=2).astype(F)
+
+
+def shell_fabric(width: int = 512, height: int = 512, spp: int = 16, grid: int = 96, layers: int = 16,
+                 disp_scale: float = 0.012, tiling: float = 6.0, tex_res: int = 256, max_depth: int = 0,
+                 seed: int = 5) -> SceneDesc:
+    """Displacement-mapped fabric by shell mapping, after the reference's
+    displacement sandbox (a cloth under GlossyWithHighLight((0.8, 0.2, 0.2), 1, 2,
+    10, 0.05) with 16 shell layers in a Cornell-style room lit from the ceiling):
+    a draped grid x grid cloth patch whose texcoords tile a plain-weave height map
+    `tiling` times, layers copies up to disp_scale along the normals, inside a
+    unit room with a 0.4 x 0.4 ceiling light. Reference integrator defaults
+    (no depth limit, Russian roulette after 5 at 0.9) unless max_depth is set."""
+    from .scene import GLOSSY_HIGHLIGHT
+    s = SceneDesc(name="shell_fabric", width=width, height=height, spp=spp,
+                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed))
+    white = s.diffuse([0.6, 0.6, 0.6])
+    red = s.diffuse([0.8, 0.1, 0.1])
+    green = s.diffuse([0.1, 0.8, 0.1])
+    walls = [
+        (quad([0, 0, 0], [1, 0, 0], [1, 0, 1], [0, 0, 1]), white),   # floor
+        (quad([0, 1, 0], [0, 1, 1], [1, 1, 1], [1, 1, 0]), white),   # ceiling
+        (quad([0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]), white),   # back
+        (quad([0, 0, 0], [0, 0, 1], [0, 1, 1], [0, 1, 0]), red),     # left
+        (quad([1, 0, 0], [1, 1, 0], [1, 1, 1], [1, 0, 1]), green),   # right
+    ]
+    for (pos, idx), mat in walls:
+        s.add_object(s.add_mesh(pos, idx), mat)
+    lo, hi, y = 0.3, 0.7, 0.999
+    lp, li = quad([lo, y, lo], [hi, y, lo], [hi, y, hi], [lo, y, hi])  # normal -y
+    s.add_object(s.add_mesh(lp, li), s.emission([8.0, 8.0, 7.6]))
+    # draped cloth: gentle folds over [0.1, 0.9]^2 at y ~ 0.1
+    g = np.linspace(0.0, 1.0, grid, dtype=np.float64)
+    xx, zz = np.meshgrid(g, g)
+    hts = 0.06 * np.sin(2.5 * np.pi * xx + 0.7) * np.cos(1.5 * np.pi * zz) + 0.1
+    heights = hts.astype(F)
+    pos, uv, idx = heightfield_mesh(heights)
+    pos = pos.copy()
+    pos[:, 0] = 0.1 + 0.8 * pos[:, 0]
+    pos[:, 2] = 0.1 + 0.8 * pos[:, 2]
+    nrm, tan, bit = heightfield_frames(heights * F(1.0 / 0.8), extent=1.0)
+    disp = s.add_texture(weave_displacement(tex_res), clamp=False, filter=True)
+    cloth = s.add_mesh_shell(pos, idx, uv * F(tiling), nrm, tan, bit, disp, disp_scale, layers)
+    s.add_object(cloth, s.add_material(GLOSSY_HIGHLIGHT, [0.8, 0.2, 0.2, 1.0, 1.0, 1.0, 2.0, 10.0, 0.05]))
+    s.set_camera(look_at((0.5, 0.55, -0.35), (0.5, 0.08, 0.5), (0, 1, 0)), 40.0 * math.pi / 180.0, height / width)
+    return s
