@@ -76,7 +76,10 @@ def parse():
     p.add_argument("--no-guided", action="store_true")
     p.add_argument("--guided-res", type=int, default=512)
     p.add_argument("--guided-seconds", type=float, default=8.0)
-    p.add_argument("--guided-ref-spp", type=int, default=2048)
+    p.add_argument("--guided-ref-spp", type=int, default=8192)
+    p.add_argument("--guided-pass-spp", type=int, default=16)
+    p.add_argument("--guided-train-pass-spp", type=int, default=4)
+    p.add_argument("--guided-max-steps", type=int, default=512)
     return p.parse_args()
 
 
@@ -249,7 +252,9 @@ def guided_equal_time(ctx, args):
     ref, noise = guiding.reference_halves(ctx, builder, desc, args.guided_ref_spp)
     t_ref = time.perf_counter() - t0
     out = guiding.equal_time_comparison(ctx, desc, time_s=args.guided_seconds, reference=ref, reference_noise=noise,
-                                        builder=builder, pass_spp=4, train_pass_spp=1)
+                                        builder=builder, pass_spp=args.guided_pass_spp,
+                                        train_pass_spp=args.guided_train_pass_spp,
+                                        max_steps_per_call=args.guided_max_steps)
     out.pop("images")
     out["workload"] = (f"occluded room ({desc.n_tris} triangles), {res}x{res} film, reference defaults "
                        f"(no depth limit, RR after 5 at 0.9)")

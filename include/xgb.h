@@ -326,15 +326,16 @@ xgb_status xgb_guide_sample(xgb_guide* guide, int n, const float* pos, const flo
 xgb_status xgb_guide_train_batch(xgb_guide* guide, int n, const float* pos, const float* nrm, const float* wo,
                                  const float* wi, const float* pdf, const float* radiance, float lr, float* loss);
 /* In-render training (xgb_scene_set_guide with train = 1): a guided vertex of a
- * camera path becomes a training record (at a rate that spreads about 2^20
+ * camera path becomes a training record (at a rate that spreads about 2^22
  * records over the call); when every path of the call has finished, a record's
  * target is the incident radiance along its sampled direction (the path's
  * later contributions divided by its throughput after the vertex), times the
  * luminance of bsdfCos there when product_target = 1 (default). Records that
  * carry radiance are pooled and consumed in Adam steps of batch_rows records
  * (default 8192, a multiple of 64, at most 65536), at most max_steps_per_call
- * (default 64) at the end of each call; a remainder smaller than a batch stays
- * pooled for the next call. */
+ * (default 512) at the end of each call; a remainder smaller than a batch stays
+ * pooled for the next call. The pool holds 2^22 records; a call that finds more
+ * than max_steps_per_call batches drops the excess. */
 xgb_status xgb_guide_set_training(xgb_guide* guide, int batch_rows, int max_steps_per_call, int product_target);
 /* Adam steps taken so far (explicit and in-render). */
 xgb_status xgb_guide_train_steps(xgb_guide* guide, uint64_t* out);

@@ -566,7 +566,7 @@ class Guide:
                        "sample")
         return dirs, pdf
 
-    def set_training(self, batch_rows: int = 8192, max_steps_per_call: int = 64, product: bool = True):
+    def set_training(self, batch_rows: int = 8192, max_steps_per_call: int = 512, product: bool = True):
         self.ctx.check(self.ctx.lib.xgb_guide_set_training(self.h, batch_rows, max_steps_per_call, int(product)),
                        "set_training")
 

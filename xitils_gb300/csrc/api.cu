@@ -152,7 +152,7 @@ struct xgb_guide {
     unsigned int* recCount = nullptr;       // [0] arena count, [3] pool count
     GuideRecord* batchRec = nullptr;        // device staging for xgb_guide_train_batch
     unsigned int* hostPoolCount = nullptr;  // pinned copy of the pool count
-    int maxStepsPerCall = 64;
+    int maxStepsPerCall = 512;
     int product = 1;                        // target: radiance x bsdfCos (1) or radiance (0)
 };
 
@@ -1227,7 +1227,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
         XGB_CUDA(ctx, cudaStreamSynchronize(st));
         int n = guidePoolTrain(gd->g, *gd->hostPoolCount, gb, s->guideLr, gd->maxStepsPerCall, st);
         guideSteps += (uint64_t)n;
-        launches += 2 + 17 * (uint64_t)n + 1;
+        launches += 2 + 2 * (uint64_t)n + 1;  // finalize, collect; two per Adam step; pool count
         XGB_CUDA(ctx, cudaGetLastError());
     }
     const Ctrl& c = *s->ctrlHost;
@@ -1413,11 +1413,11 @@ xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
     g.scratch.Y = (float*)A(4 * (size_t)R * kGuideOutPad);
     g.scratch.partial = (float*)A(guidePartialBytes());
     g.scratch.scalars = (float*)A(16);
-    gd->arenaCap = 1 << 20;
+    gd->arenaCap = 1 << 22;
     gd->arena = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)gd->arenaCap);
     gd->recCount = (unsigned int*)A(4 * 4);
     gd->batchRec = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)R);
-    g.poolCap = 8 * R;
+    g.poolCap = 1 << 22;
     g.batch = 8192;
     g.pool = (GuideRecord*)A(sizeof(GuideRecord) * (size_t)g.poolCap);
     g.poolCount = gd->recCount + 3;

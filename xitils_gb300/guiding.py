@@ -80,7 +80,7 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
                           reference_spp: int = 16384, pass_spp: int = 1, bsdf_fraction: float = 0.5,
                           lr: float = 1e-3, reference: Optional[np.ndarray] = None, seed: int = 0,
                           batch_rows: int = 8192, builder=None, train_pass_spp: int = 1,
-                          reference_noise: Optional[float] = None) -> dict:
+                          reference_noise: Optional[float] = None, max_steps_per_call: int = 512) -> dict:
     """Both arms are warmed up by one untimed pass; the guided arm's clock
     includes its network inference and every training step. Training passes
     take train_pass_spp samples (one network update per pass), the rest pass_spp."""
@@ -96,7 +96,7 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
     builder.scene.setGuide(warm, bsdf_fraction, train=True, lr=lr)
     _warm_up(ctx, builder, desc, params, pass_spp)
     guide = api.Guide(ctx, seed=seed)
-    guide.set_training(batch_rows)
+    guide.set_training(batch_rows, max_steps_per_call)
     state = {"training": True}
     builder.scene.setGuide(guide, bsdf_fraction, train=True, lr=lr)
 
@@ -115,6 +115,7 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
     return {
         "time_s": time_s, "train_fraction": train_fraction, "bsdf_fraction": bsdf_fraction,
         "pass_spp": pass_spp, "train_pass_spp": train_pass_spp, "learning_rate": lr, "batch_rows": batch_rows,
+        "max_steps_per_call": max_steps_per_call,
         "reference_relmse_estimate": reference_noise,
         "relmse_ratio_reference_noise_removed": corrected,
         "plain": {"spp": plain_spp, "seconds": plain_t, "relmse": rp, "mse": float(np.mean((plain - ref) ** 2))},
