@@ -62,7 +62,7 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="xgb", choices=["xgb", "reference"])
-    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell", "shell", "batch", "mfnm"])
+    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell", "shell", "svbrdf", "batch", "mfnm"])
     p.add_argument("--shell-grid", type=int, default=256)
     p.add_argument("--mfnm-res", type=int, default=2048)
     p.add_argument("--mfnm-ref-spp", type=int, default=2048)
@@ -99,13 +99,16 @@ def make_workload(args):
                  f"max depth 10, GGX per-texel roughness, lat-long env 1024x512")
         meta = {"data": "synthetic (seeded fBm terrain, procedural lat-long environment)", "kernel": SINGLE_KERNEL,
                 "l2": big}
-    elif args.workload == "shell":
+    elif args.workload in ("shell", "svbrdf"):
         res = args.res or 1024
         spp = args.spp or 16
         grid = args.shell_grid
-        desc = scenes.shell_fabric(res, res, spp, grid=grid, layers=16, tex_res=1024)
-        label = (f"shell-mapped fabric: {grid}x{grid} cloth grid x 16 layers ({desc.n_tris} tris), 1024^2 weave "
-                 f"displacement map, Cornell-style room, {res}x{res} film, {spp} spp, reference defaults "
+        desc = scenes.shell_fabric(res, res, spp, grid=grid, layers=16, tex_res=1024, method=args.workload)
+        how = ("1024^2 weave displacement map" if args.workload == "shell" else
+               "1024^2 weave displacement map downsampled 8x with a 4-lobe vMF SVNDF per low texel, "
+               "MultiLobeSVBRDF over the base material")
+        label = (f"shell-mapped fabric: {grid}x{grid} cloth grid x 16 layers ({desc.n_tris} tris), {how}, "
+                 f"Cornell-style room, {res}x{res} film, {spp} spp, reference defaults "
                  f"(no depth limit, RR after 5 at 0.9)")
         meta = {"data": "synthetic (seeded cloth patch, procedural plain-weave displacement map)",
                 "kernel": "k_extend (two-level closest-hit traversal with the shell-mapping discard, persistent)",
@@ -195,6 +198,30 @@ def cpu_reference_sample(desc, res, spp, nthreads, chk=None):
     port.render_pcg(d, spp_count=spp, nthreads=nthreads)
     sec = time.perf_counter() - t0
     return res * res * spp / sec / 1e6, sec, "port"
+
+
+def svndf_fit_timing(api, ctx, desc):
+    """GPU SVNDF fit of the workload's displacement map (xgb_svndf_create, one warp per
+    low texel) against the same fit on the host: the oracle's restatement on all
+    cores (OpenMP over texels, as the reference's precomputation runs)."""
+    from oracle.bindings import CpuChecker
+    src, scale, rate, seed = next(t.svndf for t in desc.textures if t.svndf is not None)
+    rgb = desc.textures[src].rgb
+    tex = api.Texture(ctx, rgb, warpClamp=desc.textures[src].clamp)
+    api.Svndf(ctx, tex, scale, rate, seed)  # first call: module load
+    times = []
+    for _ in range(3):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        api.Svndf(ctx, tex, scale, rate, seed)  # synchronises before returning
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    CpuChecker("port").svndf_fit(rgb, scale, rate, seed, desc.textures[src].clamp)
+    cpu_s = time.perf_counter() - t0
+    h, w = rgb.shape[:2]
+    return {"map": f"{w}x{h}", "rate": rate, "low_texels": ((w + rate - 1) // rate) * ((h + rate - 1) // rate),
+            "gpu_ms": 1e3 * min(times), "cpu_ms": 1e3 * cpu_s, "cpu_cores": os.cpu_count(),
+            "cpu_kind": "oracle restatement of the reference's fit, OpenMP over texels"}
 
 
 def peaks():
@@ -390,6 +417,7 @@ def run_xgb(args):
     desc, label, meta = make_workload(args)
     ctx = api.Context(local)
     builder = api.load_scene(ctx, desc)
+    svndf_fit = svndf_fit_timing(api, ctx, desc) if args.workload == "svbrdf" and rank == 0 else None
     scene = builder.scene
     W, H, spp = desc.width, desc.height, desc.spp
     rt = api.RenderTarget(ctx, W, H)
@@ -522,6 +550,8 @@ def run_xgb(args):
         "render_stats": agg,
         "guided_equal_time": guided,
     }
+    if svndf_fit is not None:
+        out["svndf_fit"] = svndf_fit
     print(json.dumps(out))
     if dist:
         dist.destroy_process_group()

@@ -141,6 +141,42 @@ xgb_status xgb_material_mf_normalmap(xgb_ctx* ctx, const xgb_material* base, xgb
 xgb_status xgb_material_set_normalmap(xgb_material* mat, const xgb_texture* normalmap);
 xgb_status xgb_material_destroy(xgb_material* mat);
 
+/* ------------------------------------------ SVNDF (prefiltered displacement) */
+/* downsampleDisplacementTexture(displacement, scale, svndf) and SVNDF
+ * (Sandbox/PrefilteringForRenderingDisplacementMappedSurfaces/Main.cpp:361-470), on
+ * the GPU: low texel (px, py) covers the rate x rate source texels from
+ * (px * rate, py * rate); its height is their mean red value and its normal
+ * distribution a 4-lobe vMF mixture fitted by the reference's EM
+ * (VonMisesFisherDistribution<4>::approximateBySEM, VonMisesFisherDistribution.h:68-160)
+ * to their normals normalize(-dh/du * scale, -dh/dv * scale, 1) (central
+ * differences, Texture.h:105-111). The fit of low texel t starts from lobes drawn
+ * from the PCG stream (t, 0, seed); the reference draws them from one sampler per
+ * OpenMP thread. rate in [1, 16]. *low receives the low-resolution height texture
+ * (red channel; bilinear; the source's clamp / wrap mode), which the caller
+ * destroys with xgb_texture_destroy. */
+typedef struct xgb_svndf xgb_svndf;
+xgb_status xgb_svndf_create(xgb_ctx* ctx, const xgb_texture* displacement, float displacement_scale, int rate,
+                            uint32_t seed, xgb_svndf** out, xgb_texture** low);
+xgb_status xgb_svndf_destroy(xgb_svndf* svndf);
+/* Size of the SVNDF (the low texture's width and height). */
+xgb_status xgb_svndf_size(const xgb_svndf* svndf, int* width, int* height);
+/* Fitted lobes, float[height][width][4][5] = mu.xyz, kappa, alpha. */
+xgb_status xgb_svndf_get_lobes(const xgb_svndf* svndf, float* host);
+/* Replaces the lobes (same layout), e.g. with a fit stored earlier; scenes built
+ * with materials on this SVNDF see the new lobes at their next render. */
+xgb_status xgb_svndf_set_lobes(xgb_svndf* svndf, const float* host);
+/* MultiLobeSVBRDF(base, lowDisplacement, scale, svndf) (Main.cpp:472-517): at each
+ * evaluation and each sample the shading normal is replaced by a normal drawn from
+ * the SVNDF at the hit's texcoord (SVNDF::sampleNormal: a stochastic bilinear
+ * choice of the texel, then the texel's mixture sampled as
+ * VonMisesFisherDistribution::sample does), in the frame of the hit's normal,
+ * tangent and bitangent; the base material is evaluated with it. getPDF is the
+ * cosine density about the unperturbed shading normal, as in the reference. The
+ * base must be a non-emissive material other than microfacet normal mapping or
+ * another MultiLobeSVBRDF; the SVNDF must outlive the material. */
+xgb_status xgb_material_multilobe_svbrdf(xgb_ctx* ctx, const xgb_material* base, const xgb_svndf* svndf,
+                                         xgb_material** out);
+
 /* ------------------------------------------------------------------- scene */
 xgb_status xgb_scene_create(xgb_ctx* ctx, xgb_scene** out);
 xgb_status xgb_scene_destroy(xgb_scene* scene);

@@ -67,12 +67,35 @@ public:
         : ctx_(ctx.get()) {
         check(xgb_texture_create(ctx_, w, h, channels, rgb, warpClamp, filter, &h_), ctx_, "Texture");
     }
+    // takes ownership of a texture the library made (the SVNDF's low-resolution map)
+    Texture(Context& ctx, xgb_texture* made) : ctx_(ctx.get()), h_(made) {}
     ~Texture() { if (h_) xgb_texture_destroy(h_); }
     const xgb_texture* get() const { return h_; }
 
 private:
     xgb_ctx* ctx_;
     xgb_texture* h_ = nullptr;
+};
+
+// SVNDF + downsampleDisplacementTexture of the displacement sandbox
+// (Sandbox/PrefilteringForRenderingDisplacementMappedSurfaces/Main.cpp:361-470),
+// fitted on the GPU; low() is the downsampled height texture.
+class SVNDF {
+public:
+    SVNDF(Context& ctx, const Texture& displacement, float displacementScale, int rate = 8, uint32_t seed = 0)
+        : ctx_(ctx.get()) {
+        xgb_texture* low = nullptr;
+        check(xgb_svndf_create(ctx_, displacement.get(), displacementScale, rate, seed, &h_, &low), ctx_, "SVNDF");
+        low_ = std::make_shared<Texture>(ctx, low);
+    }
+    ~SVNDF() { if (h_) xgb_svndf_destroy(h_); }
+    const xgb_svndf* get() const { return h_; }
+    std::shared_ptr<Texture> low() const { return low_; }
+
+private:
+    xgb_ctx* ctx_;
+    xgb_svndf* h_ = nullptr;
+    std::shared_ptr<Texture> low_;
 };
 
 class TriangleMesh {
@@ -183,6 +206,15 @@ struct MicrofacetNormalMapping : Material {
         check(xgb_material_mf_normalmap(ctx_, base->get(), &h_), ctx_, "MicrofacetNormalMapping");
     }
     std::shared_ptr<Material> base_;
+};
+// MultiLobeSVBRDF(baseMaterial, displacementTexLow, displacementScale, svndf) (Main.cpp:472-517).
+struct MultiLobeSVBRDF : Material {
+    MultiLobeSVBRDF(Context& c, std::shared_ptr<Material> base, std::shared_ptr<SVNDF> svndf)
+        : Material(c), base_(base), svndf_(svndf) {
+        check(xgb_material_multilobe_svbrdf(ctx_, base->get(), svndf->get(), &h_), ctx_, "MultiLobeSVBRDF");
+    }
+    std::shared_ptr<Material> base_;
+    std::shared_ptr<SVNDF> svndf_;
 };
 
 struct Object {

@@ -79,6 +79,35 @@ class CpuChecker:
         assert r >= 0, "add_mesh failed"
         return r
 
+    def add_svndf(self, tex, scale, rate, seed):
+        """SVNDF of texture `tex` (the displacement sandbox's downsampleDisplacementTexture);
+        returns (svndf id, id of the low-resolution height texture it appends)."""
+        low = C.c_int(-1)
+        r = self._call("add_svndf", C.c_int(tex), C.c_float(scale), C.c_int(rate), C.c_uint32(seed), C.byref(low))
+        assert r >= 0, "add_svndf failed"
+        return r, low.value
+
+    def svndf_fit(self, rgb, scale, rate, seed, clamp=True):
+        """Stand-alone fit: (low red channel [h', w'], lobes [h', w', 4, 5] = mu.xyz, kappa, alpha)."""
+        rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+        h, w = rgb.shape[:2]
+        lh, lw = (h + rate - 1) // rate, (w + rate - 1) // rate
+        low = np.zeros((lh, lw), np.float32)
+        lobes = np.zeros((lh, lw, 4, 5), np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        r = getattr(self.lib, self.p + "svndf_fit")(fp(rgb), C.c_int(w), C.c_int(h), C.c_int(int(clamp)),
+                                                    C.c_float(scale), C.c_int(rate), C.c_uint32(seed), fp(low),
+                                                    fp(lobes))
+        assert r == 0
+        return low, lobes
+
+    def vmf4_sample(self, lobes, n, seed):
+        lobes = np.ascontiguousarray(lobes, dtype=np.float32).reshape(4, 5)
+        dirs = np.zeros((n, 3), np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        assert getattr(self.lib, self.p + "vmf4_sample_pcg")(fp(lobes), C.c_int(n), C.c_uint32(seed), fp(dirs)) == 0
+        return dirs
+
     def add_mesh_shell(self, pos, idx, uv, nrm, tan, bit, tex, scale, layers):
         arrs = [_fptr(a) for a in (pos, uv, nrm, tan, bit)]
         idx = np.ascontiguousarray(idx, dtype=np.int32)

@@ -20,7 +20,10 @@ checkout into ``oracle/_ref/src`` and applies two mechanical fixes there:
 It also extracts the sandbox-only materials ``GlossyClamped`` and
 ``MicrofacetNormalMapping`` (Sandbox/MicrofacetBasedNormalMapping/Main.cpp,
 from ``enum _MethodMode`` up to ``struct MyFrameData``) into
-``oracle/_ref/src/mfnm_extract.h`` unchanged. glm, libsimdpp, Cinder and stb are
+``oracle/_ref/src/mfnm_extract.h`` unchanged, and from the displacement
+prefiltering sandbox (Sandbox/PrefilteringForRenderingDisplacementMappedSurfaces/
+Main.cpp) the ``VMFLobeNum`` constant and the classes ``SVNDF`` and
+``MultiLobeSVBRDF`` into ``oracle/_ref/src/svndf_extract.h``, unchanged. glm, libsimdpp, Cinder and stb are
 empty submodules in the reference checkout; ``oracle/shim`` stands in for them.
 
 ``oracle/_ref`` is git-ignored (no reference source enters history) but it is
@@ -51,6 +54,7 @@ HEADERS = [
     "Utils.h", "Vector.h", "VonMisesFisherDistribution.h",
 ]
 MFNM_SANDBOX = os.path.join("Sandbox", "MicrofacetBasedNormalMapping", "Main.cpp")
+PREFILTER_SANDBOX = os.path.join("Sandbox", "PrefilteringForRenderingDisplacementMappedSurfaces", "Main.cpp")
 
 CXXFLAGS = ["-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-w"]
 
@@ -88,6 +92,15 @@ def stage_reference(root: str = REFERENCE_ROOT) -> bool:
     _write(os.path.join(REF_SRC, "mfnm_extract.h"),
            "// Extracted by oracle/build_ref.py from " + MFNM_SANDBOX.replace(os.sep, "/") + "\n#pragma once\n"
            + main[start:end])
+    pre = _read(os.path.join(root, PREFILTER_SANDBOX))
+    lobes = re.search(r"^const int VMFLobeNum = \d+;$", pre, flags=re.M)
+    if lobes is None:
+        raise RuntimeError("VMFLobeNum not found in the prefiltering sandbox")
+    svndf = pre[pre.index("class SVNDF {"):pre.index("std::shared_ptr<Texture> downsampleDisplacementTexture")]
+    svbrdf = pre[pre.index("class MultiLobeSVBRDF : public Material {"):pre.index("class PrefilteredDisplaceMapping")]
+    _write(os.path.join(REF_SRC, "svndf_extract.h"),
+           "// Extracted by oracle/build_ref.py from " + PREFILTER_SANDBOX.replace(os.sep, "/") + "\n#pragma once\n"
+           + lobes.group(0) + "\n\n" + svndf + "\n" + svbrdf)
     return True
 
 
@@ -122,7 +135,8 @@ def build_ref(force: bool = False) -> str | None:
     if not os.path.isdir(os.path.join(REF_SRC, "Xitils")):
         return None
     src = os.path.join(HERE, "ref_harness.cpp")
-    deps = [src, os.path.join(HERE, "scene_api.h"), os.path.join(REF_SRC, "mfnm_extract.h")]
+    deps = [src, os.path.join(HERE, "scene_api.h"), os.path.join(REF_SRC, "mfnm_extract.h"),
+            os.path.join(REF_SRC, "svndf_extract.h")]
     if force or staged_now or not os.path.exists(REF_SO) or any(
             os.path.getmtime(d) > os.path.getmtime(REF_SO) for d in deps):
         _compile(src, REF_SO, [os.path.join(HERE, "shim"), REF_SRC, HERE], "c++20")

@@ -13,7 +13,9 @@
 //   and SkySphereUniform (SkySphere.h), StandardPathTracer / NaivePathTracer
 //   (PathTracer.h), RenderTarget / RenderTargetTile (RenderTarget.h), and the
 //   sandbox materials GlossyClamped / MicrofacetNormalMapping extracted verbatim
-//   from Sandbox/MicrofacetBasedNormalMapping/Main.cpp:13-340.
+//   from Sandbox/MicrofacetBasedNormalMapping/Main.cpp:13-340, and SVNDF /
+//   MultiLobeSVBRDF extracted verbatim from
+//   Sandbox/PrefilteringForRenderingDisplacementMappedSurfaces/Main.cpp:361-389, 472-517.
 // The harness adds, through the reference's own virtual interfaces (the way
 // the sandboxes extend it):
 //   - PcgSampler: a Sampler whose protected virtual rand() (Sampler.h:74) draws
@@ -37,6 +39,7 @@
 #include <Xitils/VonMisesFisherDistribution.h>
 
 #include "mfnm_extract.h"
+#include "svndf_extract.h"
 
 #include <chrono>
 #ifdef _OPENMP
@@ -120,9 +123,50 @@ struct RefScene {
     std::vector<std::string> textureNames;
     std::vector<std::shared_ptr<TriangleMesh>> meshes;
     std::vector<std::shared_ptr<Material>> materials;
+    std::vector<std::shared_ptr<SVNDF>> svndfs;
+    std::vector<std::shared_ptr<Texture>> svndfLow;
+    std::vector<float> svndfScale;
     bool built = false;
     int serial = 0;
 };
+
+// downsampleDisplacementTexture (Prefiltering sandbox Main.cpp:391-470) restated with
+// the reference's own Texture and VonMisesFisherDistribution<VMFLobeNum>::approximateBySEM:
+// the reference seeds one sampler per OpenMP thread (scheduling decides which texel
+// draws from which stream); here low texel t draws from the PCG stream (t, 0, seed).
+std::shared_ptr<Texture> svndfBuild(const Texture& orig, float scale, int rate, uint32_t seed, SVNDF& sv) {
+    auto low = std::make_shared<Texture>((orig.getWidth() + rate - 1) / rate, (orig.getHeight() + rate - 1) / rate);
+    low->warpClamp = orig.warpClamp;
+    sv.resolutionU = low->getWidth();
+    sv.resolutionV = low->getHeight();
+    sv.vmfs.clear();
+    sv.vmfs.resize(low->getWidth() * low->getHeight());
+    for (int py = 0; py < low->getHeight(); ++py) {
+        for (int px = 0; px < low->getWidth(); ++px) {
+            const int t = py * low->getWidth() + px;
+            PcgSampler sampler;
+            sampler.seedPath((uint32_t)t, 0, seed);
+            int count = 0;
+            std::vector<Vector3f> normals;
+            for (int ly = 0; ly < rate; ++ly) {
+                int y = py * rate + ly;
+                if (y >= orig.getHeight()) continue;
+                for (int lx = 0; lx < rate; ++lx) {
+                    int x = px * rate + lx;
+                    if (x >= orig.getWidth()) continue;
+                    Vector2f slope = Vector2f(orig.rgbDifferentialU(x, y).x, orig.rgbDifferentialV(x, y).x);
+                    Vector3f n = Vector3f(-slope.u * scale, -slope.v * scale, 1).normalize();
+                    low->r(px, py) += orig.r(x, y);
+                    normals.push_back(n);
+                    ++count;
+                }
+            }
+            low->r(px, py) /= count;
+            sv.vmfs[t] = VonMisesFisherDistribution<VMFLobeNum>::approximateBySEM(normals, sampler);
+        }
+    }
+    return low;
+}
 
 int g_serial = 0;
 
@@ -199,6 +243,54 @@ int xref_add_mesh_shell(void* p, int nV, const float* pos, const float* uv, cons
     return (int)s->meshes.size() - 1;
 }
 
+int xref_add_svndf(void* p, int tex, float scale, int rate, uint32_t seed, int* low_tex) {
+    RefScene* s = (RefScene*)p;
+    if (tex < 0 || tex >= (int)s->textures.size() || rate < 1 || !low_tex) return -1;
+    auto sv = std::make_shared<SVNDF>();
+    auto low = svndfBuild(*s->textures[tex], scale, rate, seed, *sv);
+    s->textures.push_back(low);
+    *low_tex = (int)s->textures.size() - 1;
+    s->svndfs.push_back(sv);
+    s->svndfLow.push_back(low);
+    s->svndfScale.push_back(scale);
+    return (int)s->svndfs.size() - 1;
+}
+
+int xref_svndf_fit(const float* rgb, int w, int h, int wrap_clamp, float scale, int rate, uint32_t seed,
+                   float* low_r, float* lobes) {
+    if (!rgb || w <= 0 || h <= 0 || rate < 1) return -1;
+    Texture t(w, h);
+    for (int i = 0; i < w * h * 3; ++i) t[i] = rgb[i];
+    t.warpClamp = wrap_clamp != 0;
+    SVNDF sv;
+    auto low = svndfBuild(t, scale, rate, seed, sv);
+    for (size_t i = 0; i < sv.vmfs.size(); ++i) {
+        low_r[i] = low->r((int)(i % low->getWidth()), (int)(i / low->getWidth()));
+        for (int j = 0; j < VMFLobeNum; ++j) {
+            float* o = lobes + (i * VMFLobeNum + j) * 5;
+            o[0] = sv.vmfs[i].mu[j].x; o[1] = sv.vmfs[i].mu[j].y; o[2] = sv.vmfs[i].mu[j].z;
+            o[3] = sv.vmfs[i].kappa[j]; o[4] = sv.vmfs[i].alpha[j];
+        }
+    }
+    return 0;
+}
+
+int xref_vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs) {
+    VonMisesFisherDistribution<4> v;
+    for (int j = 0; j < 4; ++j) {
+        v.mu[j] = Vector3f(lobes[5 * j], lobes[5 * j + 1], lobes[5 * j + 2]);
+        v.kappa[j] = lobes[5 * j + 3];
+        v.alpha[j] = lobes[5 * j + 4];
+    }
+    PcgSampler sampler;
+    for (int i = 0; i < n; ++i) {
+        sampler.seedPath((uint32_t)i, 0, seed);
+        Vector3f d = v.sample(sampler);
+        dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    }
+    return 0;
+}
+
 int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
     RefScene* s = (RefScene*)p;
     std::shared_ptr<Material> m;
@@ -236,6 +328,10 @@ int xref_add_material(void* p, int type, const float* f, int base, int tex, int 
     case ORC_MAT_MF_NORMALMAP:
         if (base < 0 || base >= (int)s->materials.size()) return -1;
         m = std::make_shared<MicrofacetNormalMapping>(s->materials[base]);
+        break;
+    case ORC_MAT_MULTILOBE_SVBRDF:
+        if (base < 0 || base >= (int)s->materials.size() || tex < 0 || tex >= (int)s->svndfs.size()) return -1;
+        m = std::make_shared<MultiLobeSVBRDF>(s->materials[base], s->svndfLow[tex], s->svndfScale[tex], s->svndfs[tex]);
         break;
     default: return -1;
     }

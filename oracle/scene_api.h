@@ -29,7 +29,8 @@ enum {
     ORC_MAT_SPECULAR_REFLECTION = 6,
     ORC_MAT_SPECULAR_REFRACTION = 7, /* f: index */
     ORC_MAT_SPECULAR_FRESNEL = 8,    /* f: index */
-    ORC_MAT_MF_NORMALMAP = 9         /* base: material id of the facet material                   */
+    ORC_MAT_MF_NORMALMAP = 9,        /* base: material id of the facet material                   */
+    ORC_MAT_MULTILOBE_SVBRDF = 10    /* base: material id; tex: SVNDF id (add_svndf)              */
 };
 
 enum { ORC_SKY_NONE = 0, ORC_SKY_UNIFORM = 1, ORC_SKY_PROBE = 2, ORC_SKY_LATLONG = 3 };
@@ -45,6 +46,10 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
     int P##add_mesh_shell(void* s, int nV, const float* pos, const float* uv, const float* nrm,    \
                           const float* tan, const float* bit, int nIdx, const int32_t* idx,        \
                           int tex, float scale, int layers);                                       \
+    int P##add_svndf(void* s, int tex, float scale, int rate, uint32_t seed, int* low_tex);         \
+    int P##svndf_fit(const float* rgb, int w, int h, int wrap_clamp, float scale, int rate,          \
+                     uint32_t seed, float* low_r, float* lobes);                                     \
+    int P##vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs);                  \
     int P##add_material(void* s, int type, const float* f, int base, int tex, int normalmap);      \
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \

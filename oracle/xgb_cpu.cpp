@@ -32,16 +32,22 @@
 namespace {
 
 #ifdef XGB_ORACLE_ULP_PERTURB
-// Sensitivity probe (tests only): every nonzero cosf / sinf / powf result moves one
-// ulp toward zero, the size of the difference between two libm implementations
-// (toward zero so that |cos| and |sin| never exceed 1).
+// Sensitivity probe (tests only): every nonzero cosf / sinf / powf / expf / logf /
+// asinf result moves one ulp toward zero, the size of the difference between two
+// libm implementations (toward zero so that |cos| and |sin| never exceed 1).
 inline float towardZero(float r) { return r == 0.0f ? r : std::nextafter(r, 0.0f); }
 inline float perturbedCos(float x) { return towardZero(std::cos(x)); }
 inline float perturbedSin(float x) { return towardZero(std::sin(x)); }
 inline float perturbedPow(float x, float y) { return towardZero(std::pow(x, y)); }
+inline float perturbedExp(float x) { return towardZero(std::exp(x)); }
+inline float perturbedLog(float x) { return towardZero(std::log(x)); }
+inline float perturbedAsin(float x) { return towardZero(std::asin(x)); }
 #define cosf perturbedCos
 #define sinf perturbedSin
 #define powf perturbedPow
+#define expf perturbedExp
+#define logf perturbedLog
+#define asinf perturbedAsin
 #endif
 
 const float kPi = (float)M_PI;  // Utils.h:32
@@ -531,6 +537,180 @@ struct Shading {
     float getPDF(int mi, const Isect& is, V3 wi) const;
 };
 
+// ---- vMF mixture with 4 lobes and the SVNDF of the displacement sandbox ------
+// VonMisesFisherDistribution<4> (VonMisesFisherDistribution.h): vMF() (:205-211),
+// approximateBySEM (:68-160, E-step without the lobe weights, convergence test on a
+// signed difference, both as in the reference) and sample() (:162-201, the
+// tangential part drawn in the unit disk, as in the reference).
+constexpr int kSvLobes = 4;
+struct Vmf4 {
+    V3 mu[kSvLobes];
+    float kappa[kSvLobes];
+    float alpha[kSvLobes];
+    Vmf4() {  // VonMisesFisherDistribution() (:21-34)
+        for (int i = 0; i < kSvLobes; ++i) { mu[i] = V3(1, 0, 0); kappa[i] = 0.0f; alpha[i] = 0.0f; }
+        alpha[0] = 1.0f;
+    }
+};
+inline float vmfLobe(V3 mu, float kappa, V3 omega) {
+    if (kappa == 0.0f) return 1.0f / (4 * (float)M_PI);
+    return kappa / (2 * (float)M_PI * (1.0f - expf(-2 * kappa))) * expf(kappa * (dot(omega, mu) - 1.0f));
+}
+Vmf4 vmf4Fit(const std::vector<V3>& samples, Rng& rng) {
+    const float KappaLimit = 1000;
+    const int StepMax = 100000;
+    const float DiffThreshold = 1e-6;
+    Vmf4 vmf;
+    const int n = (int)samples.size();
+    if (n == 1) {
+        for (int i = 0; i < kSvLobes; ++i) {
+            vmf.mu[i] = samples[0]; vmf.kappa[i] = KappaLimit; vmf.alpha[i] = i == 0 ? 1.0f : 0.0f;
+        }
+        return vmf;
+    }
+    for (int j = 0; j < kSvLobes; j++) {
+        float u = rng.randf();
+        float v = rng.randf();
+        float theta = asinf(u);
+        float phi = 2.0f * (float)M_PI * v - M_PI;
+        vmf.mu[j] = V3(cosf(theta) * cosf(phi), cosf(theta) * sinf(phi), sinf(theta));
+        vmf.kappa[j] = 0.5f;
+        vmf.alpha[j] = 1.0f / kSvLobes;
+    }
+    std::vector<float> z((size_t)n * kSvLobes);
+    Vmf4 last;
+    for (int step = 0; step < StepMax; ++step) {
+        for (int i = 0; i < n; i++) {
+            float gamma = 0.0f;
+            for (int j = 0; j < kSvLobes; j++) gamma += vmfLobe(vmf.mu[j], vmf.kappa[j], samples[i]);
+            for (int j = 0; j < kSvLobes; j++)
+                z[(size_t)i * kSvLobes + j] = gamma > 0.0f ? vmfLobe(vmf.mu[j], vmf.kappa[j], samples[i]) / gamma : 0.0f;
+        }
+        for (int j = 0; j < kSvLobes; j++) {
+            float a = 0.0f;
+            V3 r(0.0f, 0.0f, 0.0f);
+            for (int i = 0; i < n; i++) {
+                a += z[(size_t)i * kSvLobes + j];
+                r = r + z[(size_t)i * kSvLobes + j] * samples[i];
+            }
+            r = r / a;
+            a /= n;
+            vmf.alpha[j] = a;
+            vmf.kappa[j] = (3 * length(r) - powf(length(r), 3.0f)) / (1.0f - lengthSq(r));
+            vmf.mu[j] = normalize(r);
+            if (vmf.kappa[j] > KappaLimit) vmf.kappa[j] = KappaLimit;
+            if (vmf.kappa[j] < 0.0f) vmf.kappa[j] = 0.0f;
+        }
+        if (step > 0) {
+            float diff = 0.0f;
+            for (int j = 0; j < kSvLobes; ++j) {
+                diff += lengthSq(vmf.mu[j] - last.mu[j]);
+                diff += (vmf.kappa[j] - last.kappa[j]) * 0.1f;
+            }
+            if (diff < DiffThreshold) break;
+        }
+        last = vmf;
+    }
+    return vmf;
+}
+V3 vmf4Sample(const Vmf4& vmf, Rng& rng) {
+    // randiAlongNormalizedWeights (Sampler.h:52-61)
+    float uw = rng.randf();
+    float accum = 0.0f;
+    int k = 0;
+    for (; k < kSvLobes - 1; ++k) {
+        accum += vmf.alpha[k];
+        if (uw <= accum) break;
+    }
+    const V3 mu = vmf.mu[k];
+    const float kappa = vmf.kappa[k];
+    if (eq(mu, V3(0, 0, 0))) return V3(0, 0, 0);
+    float Vx, Vy, W;
+    {
+        float u = rng.randf();
+        float v = rng.randf();
+        float r = sqrtf(u);
+        float theta = 2.0f * (float)M_PI * v - M_PI;
+        Vx = r * cosf(theta);
+        Vy = r * sinf(theta);
+    }
+    {
+        float u = rng.randf();
+        if (kappa > 0.0f) W = 1.0f + powf(kappa, -1.0f) * logf(u + (1.0f - u) * std::exp(-2.0f * kappa));
+        else W = 1.0f;
+    }
+    float sq = safeSqrt(1.0f - powf(W, 2.0f));
+    Basis basis(normalize(mu));
+    return normalize(basis.toGlobal(W, sq * Vx, sq * Vy));
+}
+
+// SVNDF of a displacement map (Sandbox/PrefilteringForRenderingDisplacementMappedSurfaces/
+// Main.cpp:361-389) and its construction by downsampleDisplacementTexture (:391-470):
+// low texel (px, py) averages the red channel of its rate x rate source texels and
+// fits a 4-lobe mixture to their normals normalize(-dh/du * scale, -dh/dv * scale, 1)
+// from Texture::rgbDifferentialU / V at the texel. The reference draws the fit's
+// initial lobes from one sampler per OpenMP thread (so which stream a texel gets
+// depends on scheduling); here texel t uses the stream seeded (t, 0, seed).
+struct Svndf {
+    int resU = 0, resV = 0;
+    std::vector<Vmf4> vmfs;
+    // SVNDF::sampleNormal (:366-388): stochastic bilinear choice of the texel; the
+    // y1 wrap compares with resolutionU as the reference does (then clamped to the
+    // rows that exist, which only matters for non-square maps).
+    V3 sampleNormal(V2 uv, Rng& rng) const {
+        float nu = uv.x - floorf(uv.x), nv = uv.y - floorf(uv.y);
+        int x0 = (int)(nu * resU - 0.5f);
+        int y0 = (int)(nv * resV - 0.5f);
+        int x1 = x0 + 1, y1 = y0 + 1;
+        float wx1 = (nu * resU - 0.5f) - x0;
+        float wy1 = (nv * resV - 0.5f) - y0;
+        if (x0 < 0) x0 = resU - 1;
+        if (y0 < 0) y0 = resV - 1;
+        if (x1 >= resU) x1 = 0;
+        if (y1 >= resU) y1 = 0;
+        if (y1 >= resV) y1 = 0;
+        int x = (rng.randf() <= wx1) ? x1 : x0;
+        int y = (rng.randf() <= wy1) ? y1 : y0;
+        return vmf4Sample(vmfs[(size_t)y * resU + x], rng);
+    }
+};
+// Returns the low-resolution height texture (red channel; green and blue zero).
+Texture svndfFit(const Texture& orig, float scale, int rate, uint32_t seed, Svndf& out) {
+    Texture low;
+    low.w = (orig.w + rate - 1) / rate;
+    low.h = (orig.h + rate - 1) / rate;
+    low.clamp = orig.clamp;
+    low.filter = true;
+    low.rgb.assign((size_t)low.w * low.h * 3, 0.0f);
+    out.resU = low.w;
+    out.resV = low.h;
+    out.vmfs.assign((size_t)low.w * low.h, Vmf4());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < low.w * low.h; ++t) {
+        const int px = t % low.w, py = t / low.w;
+        int count = 0;
+        float r = 0.0f;
+        std::vector<V3> normals;
+        for (int ly = 0; ly < rate; ++ly) {
+            int y = py * rate + ly;
+            if (y >= orig.h) continue;
+            for (int lx = 0; lx < rate; ++lx) {
+                int x = px * rate + lx;
+                if (x >= orig.w) continue;
+                float su = orig.diffUAt(x, y).x, sv = orig.diffVAt(x, y).x;
+                normals.push_back(normalize(V3(-su * scale, -sv * scale, 1)));
+                r += orig.at(x, y).x;
+                ++count;
+            }
+        }
+        low.rgb[3 * (size_t)t] = r / count;
+        Rng rng;
+        rng.seed((uint32_t)t, 0, seed);
+        out.vmfs[t] = vmf4Fit(normals, rng);
+    }
+    return low;
+}
+
 struct Scene {
     std::vector<Texture> textures;
     std::vector<Mesh> meshes;
@@ -544,6 +724,7 @@ struct Scene {
     V3 skyColor;
     int skyTex = -1;
     int fixes = 0;  // opt-in quirk fixes of the render (xcpu_set_fixes)
+    std::vector<Svndf> svndfs;
     bool built = false;
 };
 
@@ -697,9 +878,21 @@ inline float G1m(V3 w, V3 wm, V3 wp, V3 wt, V3 wg) {
     return dot(w, wm) > 0.0f ? minT(1.0f, clampPositive(dot(w, wg)) / (a_p(w, wp, wg) + a_t(w, wp, wt, wg))) : 0.0f;
 }
 
+// MultiLobeSVBRDF::perturbInteraction (Prefiltering sandbox Main.cpp:502-515): the shading
+// normal replaced by a normal drawn from the SVNDF at the texcoord, expressed in the
+// frame of the (non-shading) normal, tangent and bitangent.
+Isect svbrdfPerturb(const Scene& sc, const Material& m, const Isect& is, Rng& rng) {
+    Isect p = is;
+    V3 n = sc.svndfs[m.tex].sampleNormal(is.uv, rng);
+    p.sn = normalize(n.z * is.n + n.x * is.tangent + n.y * is.bitangent);
+    return p;
+}
+
 V3 Shading::bsdfCos(int mi, const Isect& is, Rng& rng, V3 wi) const {
     const Material& m = sc->materials[mi];
     switch (m.type) {
+    case ORC_MAT_MULTILOBE_SVBRDF:  // Main.cpp:489-491
+        return bsdfCos(m.base, svbrdfPerturb(*sc, m, is, rng), rng, wi);
     case ORC_MAT_DIFFUSE:  // Material.h:59-65
         if (m.tex < 0) return m.albedo / M_PI * clampPositive(dot(is.sn, wi));
         return m.albedo / M_PI * sc->textures[m.tex].lookup(is.uv) * clampPositive(dot(is.sn, wi));
@@ -744,6 +937,7 @@ V3 Shading::bsdfCos(int mi, const Isect& is, Rng& rng, V3 wi) const {
 float Shading::getPDF(int mi, const Isect& is, V3 wi) const {
     const Material& m = sc->materials[mi];
     switch (m.type) {
+    case ORC_MAT_MULTILOBE_SVBRDF: return clampPositive(dot(is.sn, wi)) / M_PI;  // Main.cpp:497-499
     case ORC_MAT_DIFFUSE: return clampPositive(dot(wi, is.sn)) / M_PI;  // Material.h:78-81
     case ORC_MAT_METAL: {
         float r = metalRoughness(*sc, m, is);
@@ -783,6 +977,8 @@ float Shading::getPDF(int mi, const Isect& is, V3 wi) const {
 V3 Shading::evalAndSample(int mi, const Isect& is, Rng& rng, V3* wi, float* pdf) const {
     const Material& m = sc->materials[mi];
     switch (m.type) {
+    case ORC_MAT_MULTILOBE_SVBRDF:  // Main.cpp:493-495
+        return evalAndSample(m.base, svbrdfPerturb(*sc, m, is, rng), rng, wi, pdf);
     case ORC_MAT_DIFFUSE: {  // Material.h:67-76, Vector.h:817-824
         V3 n = is.sn;
         Basis basis(n);
@@ -1258,6 +1454,55 @@ int xcpu_add_mesh_shell(void* s, int nV, const float* pos, const float* uv, cons
     return (int)sc->meshes.size() - 1;
 }
 
+int xcpu_add_svndf(void* s, int tex, float scale, int rate, uint32_t seed, int* low_tex) {
+    Scene* sc = (Scene*)s;
+    if (tex < 0 || tex >= (int)sc->textures.size() || rate < 1 || !low_tex) return -1;
+    Svndf sv;
+    Texture low = svndfFit(sc->textures[tex], scale, rate, seed, sv);
+    sc->textures.push_back(std::move(low));
+    *low_tex = (int)sc->textures.size() - 1;
+    sc->svndfs.push_back(std::move(sv));
+    return (int)sc->svndfs.size() - 1;
+}
+
+// Stand-alone fit for tests: low red channel [ceil(h/rate)][ceil(w/rate)] and, per low
+// texel, 4 lobes x (mu.xyz, kappa, alpha).
+int xcpu_svndf_fit(const float* rgb, int w, int h, int wrap_clamp, float scale, int rate, uint32_t seed,
+                   float* low_r, float* lobes) {
+    if (!rgb || w <= 0 || h <= 0 || rate < 1) return -1;
+    Texture t;
+    t.w = w; t.h = h; t.clamp = wrap_clamp != 0; t.filter = true;
+    t.rgb.assign(rgb, rgb + (size_t)w * h * 3);
+    Svndf sv;
+    Texture low = svndfFit(t, scale, rate, seed, sv);
+    for (size_t i = 0; i < sv.vmfs.size(); ++i) {
+        low_r[i] = low.rgb[3 * i];
+        for (int j = 0; j < kSvLobes; ++j) {
+            float* o = lobes + (i * kSvLobes + j) * 5;
+            o[0] = sv.vmfs[i].mu[j].x; o[1] = sv.vmfs[i].mu[j].y; o[2] = sv.vmfs[i].mu[j].z;
+            o[3] = sv.vmfs[i].kappa[j]; o[4] = sv.vmfs[i].alpha[j];
+        }
+    }
+    return 0;
+}
+
+// Directions drawn from a 4-lobe mixture (lobes: 4 x (mu.xyz, kappa, alpha)), one PCG
+// stream (i, 0, seed) per draw.
+int xcpu_vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs) {
+    Vmf4 v;
+    for (int j = 0; j < kSvLobes; ++j) {
+        v.mu[j] = V3(lobes[5 * j], lobes[5 * j + 1], lobes[5 * j + 2]);
+        v.kappa[j] = lobes[5 * j + 3]; v.alpha[j] = lobes[5 * j + 4];
+    }
+    for (int i = 0; i < n; ++i) {
+        Rng rng;
+        rng.seed((uint32_t)i, 0, seed);
+        V3 d = vmf4Sample(v, rng);
+        dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    }
+    return 0;
+}
+
 int xcpu_add_material(void* s, int type, const float* f, int base, int tex, int normalmap) {
     Scene* sc = (Scene*)s;
     Material m;
@@ -1277,6 +1522,9 @@ int xcpu_add_material(void* s, int type, const float* f, int base, int tex, int 
     case ORC_MAT_SPECULAR_FRESNEL: m.index = f[0]; break;
     case ORC_MAT_MF_NORMALMAP:
         if (base < 0 || base >= (int)sc->materials.size()) return -1;
+        break;
+    case ORC_MAT_MULTILOBE_SVBRDF:  // base material and SVNDF (index in tex)
+        if (base < 0 || base >= (int)sc->materials.size() || tex < 0 || tex >= (int)sc->svndfs.size()) return -1;
         break;
     default: return -1;
     }

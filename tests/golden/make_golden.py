@@ -11,7 +11,10 @@ per-(pixel, sample) PCG streams and stores
                         checker-masked hemisphere sample set built the way
                         Sandbox/VonMisesFisherDistribution/Main.cpp:71-82 builds
                         its set (numpy seeded draws here), with the fitted
-                        mixture's pdf at random directions.
+                        mixture's pdf at random directions; and the SVNDF fit
+                        (the displacement sandbox's downsampling with
+                        VonMisesFisherDistribution<4>::approximateBySEM per
+                        low texel) of a plain-weave height map.
 Usage: python tests/golden/make_golden.py
 """
 import os
@@ -33,6 +36,8 @@ CASES = {
     "terrain_g65_40x40x2": (lambda: scenes.terrain(grid=65, width=40, height=40, spp=2, env_size=(128, 64)),
                             IntegratorParams()),
     "shell_fabric_g24_40x40x2": (lambda: scenes.shell_fabric(40, 40, 2, grid=24, tex_res=64), IntegratorParams()),
+    "shell_svbrdf_g20_40x40x2": (lambda: scenes.shell_fabric(40, 40, 2, grid=20, tex_res=64, method="svbrdf"),
+                                 IntegratorParams()),
 }
 
 
@@ -98,6 +103,10 @@ def main():
         aov[name + "_color"], aov[name + "_albedo"], aov[name + "_normal"] = film, albedo, normal
         print(name, float(film.mean()), float(albedo.mean()), float(normal.mean()))
     aov.update(vmf_fixture())
+    # SVNDF fit (per-texel 4-lobe EM) of the plain-weave map, wrap addressing, rate 8, seed 7
+    from oracle.bindings import CpuChecker
+    aov["svndf_low"], aov["svndf_lobes"] = CpuChecker("reference").svndf_fit(scenes.weave_displacement(64), 0.05, 8, 7,
+                                                                             False)
     print("vmf log-likelihood", float(np.mean(np.log(aov["vmf_sample_pdf"]))))
     np.savez_compressed(os.path.join(HERE, "reference_aov_vmf.npz"), **aov)
 

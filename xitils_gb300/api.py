@@ -15,8 +15,8 @@ from typing import Optional
 
 import numpy as np
 
-from .scene import (DIFFUSE, EMISSION, GLOSSY, GLOSSY_CLAMPED, GLOSSY_HIGHLIGHT, METAL, MF_NORMALMAP, NAIVE,
-                    SKY_LATLONG, SKY_NONE, SKY_PROBE, SKY_UNIFORM, SPECULAR_FRESNEL, SPECULAR_REFLECTION,
+from .scene import (DIFFUSE, EMISSION, GLOSSY, GLOSSY_CLAMPED, GLOSSY_HIGHLIGHT, METAL, MF_NORMALMAP, MULTILOBE_SVBRDF,
+                    NAIVE, SKY_LATLONG, SKY_NONE, SKY_PROBE, SKY_UNIFORM, SPECULAR_FRESNEL, SPECULAR_REFLECTION,
                     SPECULAR_REFRACTION, STANDARD, IntegratorParams)
 from .transform import Transform
 
@@ -85,6 +85,12 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_mesh_create": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(P)],
         "xgb_mesh_create_shell": [P, C.c_int, FP, FP, FP, FP, FP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), P,
                                   C.c_float, C.c_int, C.POINTER(P)],
+        "xgb_svndf_create": [P, P, C.c_float, C.c_int, C.c_uint32, C.POINTER(P), C.POINTER(P)],
+        "xgb_svndf_destroy": [P],
+        "xgb_svndf_size": [P, C.POINTER(C.c_int), C.POINTER(C.c_int)],
+        "xgb_svndf_get_lobes": [P, FP],
+        "xgb_svndf_set_lobes": [P, FP],
+        "xgb_material_multilobe_svbrdf": [P, P, P, C.POINTER(P)],
         "xgb_mesh_destroy": [P],
         "xgb_mesh_triangle_count": [P, C.POINTER(C.c_int)],
         "xgb_material_diffuse": [P, FP, P, C.POINTER(P)],
@@ -216,6 +222,34 @@ class Texture:
                   "Texture")
 
 
+class Svndf:
+    """SVNDF of a displacement texture fitted on the GPU (the displacement sandbox's
+    downsampleDisplacementTexture + SVNDF); ``low`` is the low-resolution height
+    texture it produces."""
+
+    def __init__(self, ctx: Context, displacement: Texture, displacementScale: float, rate: int = 8, seed: int = 0):
+        self.ctx = ctx
+        self.h = P()
+        low = P()
+        ctx.check(ctx.lib.xgb_svndf_create(ctx.h, displacement.h, C.c_float(displacementScale), int(rate),
+                                           C.c_uint32(seed), C.byref(self.h), C.byref(low)), "Svndf")
+        self.low = Texture.__new__(Texture)
+        self.low.ctx, self.low.h = ctx, low
+        w, h = C.c_int(), C.c_int()
+        ctx.check(ctx.lib.xgb_svndf_size(self.h, C.byref(w), C.byref(h)), "Svndf.size")
+        self.width, self.height = w.value, h.value
+
+    def lobes(self) -> np.ndarray:
+        """Fitted mixtures [height, width, 4, 5] = mu.xyz, kappa, alpha."""
+        out = np.zeros((self.height, self.width, 4, 5), np.float32)
+        self.ctx.check(self.ctx.lib.xgb_svndf_get_lobes(self.h, _fp(out)), "Svndf.lobes")
+        return out
+
+    def set_lobes(self, lobes: np.ndarray):
+        lobes = _f32(lobes).reshape(self.height, self.width, 4, 5)
+        self.ctx.check(self.ctx.lib.xgb_svndf_set_lobes(self.h, _fp(lobes)), "Svndf.set_lobes")
+
+
 class TriangleMesh:
     """xitils::TriangleMesh; setGeometry copies the arrays and builds its BVH on the GPU."""
 
@@ -322,6 +356,14 @@ class MicrofacetNormalMapping(Material):
     def __init__(self, ctx, base: Material):
         super().__init__(ctx, ctx.lib.xgb_material_mf_normalmap, base.h)
         self.base = base
+
+
+class MultiLobeSVBRDF(Material):
+    """MultiLobeSVBRDF(base, lowDisplacement, scale, svndf) of the displacement sandbox."""
+
+    def __init__(self, ctx, base: Material, svndf: Svndf):
+        super().__init__(ctx, ctx.lib.xgb_material_multilobe_svbrdf, base.h, svndf.h)
+        self.base, self.svndf = base, svndf
 
 
 class PinholeCamera:
@@ -588,12 +630,18 @@ class GpuSceneBuilder:
     """Backend for ``SceneDesc.emit``: replays a recorded scene into the GPU library."""
 
     KIND_MAKERS = {DIFFUSE, METAL, GLOSSY, GLOSSY_HIGHLIGHT, GLOSSY_CLAMPED, EMISSION, SPECULAR_REFLECTION,
-                   SPECULAR_REFRACTION, SPECULAR_FRESNEL, MF_NORMALMAP}
+                   SPECULAR_REFRACTION, SPECULAR_FRESNEL, MF_NORMALMAP, MULTILOBE_SVBRDF}
 
     def __init__(self, ctx: Context):
         self.ctx = ctx
         self.scene = Scene(ctx)
-        self.textures, self.meshes, self.materials = [], [], []
+        self.textures, self.meshes, self.materials, self.svndfs = [], [], [], []
+
+    def add_svndf(self, tex, scale, rate, seed):
+        sv = Svndf(self.ctx, self.textures[tex], scale, rate, seed)
+        self.svndfs.append(sv)
+        self.textures.append(sv.low)
+        return len(self.svndfs) - 1, len(self.textures) - 1
 
     def add_texture(self, rgb, clamp=True, filter=True):
         self.textures.append(Texture(self.ctx, rgb, clamp, filter))
@@ -633,6 +681,8 @@ class GpuSceneBuilder:
             m = SpecularFresnel(ctx, f[0])
         elif kind == MF_NORMALMAP:
             m = MicrofacetNormalMapping(ctx, self.materials[base])
+        elif kind == MULTILOBE_SVBRDF:
+            m = MultiLobeSVBRDF(ctx, self.materials[base], self.svndfs[tex])
         else:
             raise ValueError(kind)
         if normalmap >= 0:

@@ -126,12 +126,19 @@ struct xgb_mesh {
     int shellLayers = 0, shellFaces = 0;
 };
 
+struct xgb_svndf {
+    xgb_ctx* ctx;
+    int resU = 0, resV = 0;
+    float4* lobes = nullptr;  // 5 float4 per low texel (SvndfDev)
+};
+
 struct xgb_material {
     xgb_ctx* ctx;
     Material m;
     const xgb_texture* tex = nullptr;
     const xgb_texture* normalmap = nullptr;
     const xgb_material* base = nullptr;
+    const xgb_svndf* svndf = nullptr;  // MultiLobeSVBRDF
 };
 
 struct xgb_film {
@@ -590,6 +597,111 @@ xgb_status xgb_material_mf_normalmap(xgb_ctx* ctx, const xgb_material* base, xgb
     m->base = base;
     return XGB_OK;
 }
+xgb_status xgb_material_multilobe_svbrdf(xgb_ctx* ctx, const xgb_material* base, const xgb_svndf* svndf,
+                                         xgb_material** out) {
+    if (!base || !svndf || base->m.kind == MAT_MF_NORMALMAP || base->m.kind == MAT_EMISSION ||
+        base->m.kind == MAT_MULTILOBE_SVBRDF)
+        return fail(ctx, XGB_INVALID_ARG,
+                    "xgb_material_multilobe_svbrdf: needs an SVNDF and a non-emissive base other than MFNM / SVBRDF");
+    xgb_material* m;
+    xgb_status st = newMaterial(ctx, MAT_MULTILOBE_SVBRDF, out, &m);
+    if (st) return st;
+    m->base = base;
+    m->svndf = svndf;
+    return XGB_OK;
+}
+
+xgb_status xgb_svndf_create(xgb_ctx* ctx, const xgb_texture* displacement, float displacement_scale, int rate,
+                            uint32_t seed, xgb_svndf** out, xgb_texture** low) {
+    if (!ctx || !out || !low) return XGB_INVALID_ARG;
+    if (!displacement || rate < 1 || rate > 16 || !std::isfinite(displacement_scale))
+        return fail(ctx, XGB_INVALID_ARG, "xgb_svndf_create: needs a displacement texture and rate in [1, 16]");
+    cudaSetDevice(ctx->device);
+    const int W = (displacement->w + rate - 1) / rate, H = (displacement->h + rate - 1) / rate;
+    auto* sv = new xgb_svndf();
+    sv->ctx = ctx;
+    sv->resU = W;
+    sv->resV = H;
+    auto* tex = new xgb_texture();
+    tex->ctx = ctx;
+    tex->w = W; tex->h = H; tex->clamp = displacement->clamp; tex->filter = 1;  // Texture(w, h): bilinear
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMalloc((void**)&sv->lobes, sizeof(float4) * 5 * (size_t)W * H);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&tex->d, sizeof(float4) * (size_t)W * H);
+    if (e == cudaSuccess) {
+        const TextureDev src{displacement->d, displacement->w, displacement->h, displacement->clamp, displacement->filter};
+        e = svndfFit(src, displacement_scale, rate, seed, W, H, sv->lobes, tex->d, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        dfree(sv->lobes);
+        dfree(tex->d);
+        delete sv;
+        delete tex;
+        return e == cudaErrorMemoryAllocation ? fail(ctx, XGB_OOM, "xgb_svndf_create: out of device memory")
+                                              : cudaFail(ctx, e, "xgb_svndf_create");
+    }
+    *out = sv;
+    *low = tex;
+    return XGB_OK;
+}
+
+xgb_status xgb_svndf_destroy(xgb_svndf* svndf) {
+    if (!svndf) return XGB_INVALID_ARG;
+    dfree(svndf->lobes);
+    delete svndf;
+    return XGB_OK;
+}
+
+xgb_status xgb_svndf_size(const xgb_svndf* svndf, int* width, int* height) {
+    if (!svndf || !width || !height) return XGB_INVALID_ARG;
+    *width = svndf->resU;
+    *height = svndf->resV;
+    return XGB_OK;
+}
+
+xgb_status xgb_svndf_get_lobes(const xgb_svndf* svndf, float* host) {
+    if (!svndf || !host) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = svndf->ctx;
+    cudaSetDevice(ctx->device);
+    const size_t T = (size_t)svndf->resU * svndf->resV;
+    std::vector<float4> raw(5 * T);
+    XGB_CUDA(ctx, cudaMemcpyAsync(raw.data(), svndf->lobes, sizeof(float4) * raw.size(), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    XGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t t = 0; t < T; ++t) {
+        const float4 al = raw[5 * t + 4];
+        const float alpha[4] = {al.x, al.y, al.z, al.w};
+        for (int j = 0; j < 4; ++j) {
+            float* o = host + (t * 4 + j) * 5;
+            const float4 l = raw[5 * t + j];
+            o[0] = l.x; o[1] = l.y; o[2] = l.z; o[3] = l.w; o[4] = alpha[j];
+        }
+    }
+    return XGB_OK;
+}
+
+xgb_status xgb_svndf_set_lobes(xgb_svndf* svndf, const float* host) {
+    if (!svndf || !host) return XGB_INVALID_ARG;
+    xgb_ctx* ctx = svndf->ctx;
+    cudaSetDevice(ctx->device);
+    const size_t T = (size_t)svndf->resU * svndf->resV;
+    std::vector<float4> raw(5 * T);
+    for (size_t t = 0; t < T; ++t) {
+        float alpha[4];
+        for (int j = 0; j < 4; ++j) {
+            const float* l = host + (t * 4 + j) * 5;
+            raw[5 * t + j] = make_float4(l[0], l[1], l[2], l[3]);
+            alpha[j] = l[4];
+        }
+        raw[5 * t + 4] = make_float4(alpha[0], alpha[1], alpha[2], alpha[3]);
+    }
+    XGB_CUDA(ctx, cudaMemcpyAsync(svndf->lobes, raw.data(), sizeof(float4) * raw.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    XGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return XGB_OK;
+}
+
 xgb_status xgb_material_set_normalmap(xgb_material* mat, const xgb_texture* normalmap) {
     if (!mat) return XGB_INVALID_ARG;
     mat->normalmap = normalmap;
@@ -808,12 +920,18 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
         inst[i].identity = isIdentity(o.mat) && isIdentity(o.matInv) ? 1 : 0;
         boxes[i] = transformBox(o.mat, o.mesh->bound);
     }
+    std::map<const xgb_svndf*, int> svIds;
+    std::vector<SvndfDev> sv;
     std::vector<Material> dm(mats.size());
     for (size_t i = 0; i < mats.size(); ++i) {
         dm[i] = mats[i]->m;
         dm[i].tex = texId(mats[i]->tex);
         dm[i].normalmap = texId(mats[i]->normalmap);
         dm[i].base = mats[i]->base ? matIds[mats[i]->base] : -1;
+        if (const xgb_svndf* d = mats[i]->svndf) {  // MultiLobeSVBRDF: tex = index in the SVNDF table
+            if (!svIds.count(d)) { svIds[d] = (int)sv.size(); sv.push_back(SvndfDev{d->lobes, d->resU, d->resV}); }
+            dm[i].tex = svIds[d];
+        }
     }
     // whether any object's material takes the learned proposal (integrator.cu::guidableBasic)
     s->guidable = false;
@@ -905,6 +1023,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     };
     SceneDev& sd = s->sd;
     MeshDev* dMeshes; Instance* dInst; Node2* dTlas; Material* dMat; TextureDev* dTex = nullptr; LightDev* dLights = nullptr;
+    SvndfDev* dSv = nullptr;
     float4* dLN = nullptr; float* dLP = nullptr; float4* dBox = nullptr;
     std::vector<float4> instBox(2 * inst.size());
     for (size_t i = 0; i < inst.size(); ++i) {
@@ -916,6 +1035,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     XGB_CUDA(ctx, up(&dTlas, tlas));
     XGB_CUDA(ctx, up(&dMat, dm));
     XGB_CUDA(ctx, up(&dTex, td));
+    XGB_CUDA(ctx, up(&dSv, sv));
     XGB_CUDA(ctx, up(&dLights, lights));
     XGB_CUDA(ctx, up(&dLN, lightNormal));
     XGB_CUDA(ctx, up(&dLP, lightPdf));
@@ -928,9 +1048,12 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.blasLayout = blasLayout;
     sd.fixes = (int)s->fixes;
     sd.shell = anyShell;
+    sd.nested = 0;
+    for (const Material& m : dm) sd.nested |= (m.kind == MAT_MF_NORMALMAP || m.kind == MAT_MULTILOBE_SVBRDF) ? 1 : 0;
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;
+    sd.svndfs = dSv;
     sd.lights = dLights;
     sd.nLights = (int)lights.size();
     sd.lightNormal = dLN;

@@ -240,7 +240,7 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
     mx.lobe[4].alpha = a1.x; mx.lobe[5].alpha = a1.y; mx.lobe[6].alpha = a1.z; mx.lobe[7].alpha = a1.w;
 }
 
-template <class J>
+template <class J, bool NESTED>
 __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
                                                        ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                     if (emissive) filmAddS(rp, pix, thr * emission(mat, -dir, s.n));
                     V3 wi;
                     float pdf = pdfPrev;
-                    thr = thr * evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                    thr = thr * evalAndSampleT<NESTED>(sc, mat, s, rng, &wi, &pdf);
                     bool alive = !isZero(thr);
                     len += 1;
                     if (alive && rp.maxDepth > 0 && len > rp.maxDepth) alive = false;
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                         VmfMixture mx;
                         float fcos = 0.0f;  // luminance of bsdfCos(wi) at a guided vertex
                         if (!guidedHere) {
-                            f = evalAndSample(sc, mat, s, rng, &wi, &pdf);
+                            f = evalAndSampleT<NESTED>(sc, mat, s, rng, &wi, &pdf);
                         } else {
                             // One-sample MIS of the BSDF and the learned vMF mixture (balance
                             // heuristic): pdf = frac p_bsdf + (1 - frac) p_vmf; unbiased at any
@@ -377,16 +377,16 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                             const float frac = rp.bsdfFrac;
                             if (rng.randf() < frac) {
                                 float pb = 0.0f;
-                                V3 e = evalAndSample(sc, mat, s, rng, &wi, &pb);
+                                V3 e = evalAndSampleT<NESTED>(sc, mat, s, rng, &wi, &pb);
                                 float pm = frac * pb + (1.0f - frac) * mixturePdf(mx, wi);
                                 f = (pb > 0.0f && pm > 0.0f) ? e * (pb / pm) : V3(0.0f);
                                 fcos = luminance(e) * pb;
                                 pdf = pm;
                             } else {
                                 wi = mixtureSample(mx, rng);
-                                float pb = getPDF(sc, mat, s, wi);
+                                float pb = getPDFT<NESTED>(sc, mat, s, wi);
                                 float pm = frac * pb + (1.0f - frac) * mixturePdf(mx, wi);
-                                V3 bc = bsdfCos(sc, mat, s, rng, wi);
+                                V3 bc = bsdfCosT<NESTED>(sc, mat, s, rng, wi);
                                 f = pm > 0.0f ? bc / pm : V3(0.0f);
                                 fcos = luminance(bc);
                                 pdf = pm;
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                                 float distSq = dist * dist;
                                 float mis;
                                 if (pdf >= 0.0f) {
-                                    float pb = getPDF(sc, mat, s, sd);
+                                    float pb = getPDFT<NESTED>(sc, mat, s, sd);
                                     if (guidedHere) pb = rp.bsdfFrac * pb + (1.0f - rp.bsdfFrac) * mixturePdf(mx, sd);
                                     float cosLight = fabsf(dot(-sd, ls.sn));
                                     pb *= cosLight / distSq;
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                                 if (mis > 0.0f) {
                                     float G = fabsf(dot(-sd, ls.sn)) / distSq;
                                     Pcg spec = rng;  // bsdfCos draws only if the light is visible
-                                    V3 bc = bsdfCos(sc, mat, s, spec, sd);
+                                    V3 bc = bsdfCosT<NESTED>(sc, mat, s, spec, sd);
                                     V3 Le = emission(sc.materials[ls.material], -sd, ls.n);
                                     V3 c = thr * mis * bc * Le * G / ls.pdf;
                                     r.so = make_float4(so.x, so.y, so.z, stMax);
@@ -508,7 +508,8 @@ void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctr
 
 void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
                  Ctrl* ctrl, int grid, cudaStream_t s) {
-    k_shade<OneJob><<<grid, kShadeBlock, 0, s>>>(OneJob{sc, rp}, in, h, out, sq, ctrl);
+    if (sc.nested) k_shade<OneJob, true><<<grid, kShadeBlock, 0, s>>>(OneJob{sc, rp}, in, h, out, sq, ctrl);
+    else k_shade<OneJob, false><<<grid, kShadeBlock, 0, s>>>(OneJob{sc, rp}, in, h, out, sq, ctrl);
 }
 
 void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s) {
@@ -517,7 +518,9 @@ void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, 
 
 void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
                       cudaStream_t s) {
-    k_shade<ManyJobs><<<grid, kShadeBlock, 0, s>>>(ManyJobs{b.scenes, b.params, b.start, b.nJobs}, in, h, out, sq, ctrl);
+    const ManyJobs jobs{b.scenes, b.params, b.start, b.nJobs};
+    if (b.nested) k_shade<ManyJobs, true><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+    else k_shade<ManyJobs, false><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb

@@ -12,6 +12,9 @@
 namespace xgb {
 
 struct Surface {  // SurfaceIntersection (Interaction.h:16-32), world space
+    // stan / sbit: the shading tangent frame in object space while makeSurface
+    // applies a normal map; afterwards they are only read by MultiLobeSVBRDF, for
+    // which makeSurface leaves isect.tangent / bitangent there in world space.
     V3 p, wo, n, sn, stan, sbit;
     float2 uv;
 };
@@ -65,6 +68,53 @@ __device__ __forceinline__ float texDiff(const TextureDev& t, float u, float v) 
                (wx1 * wy1) * at(x0 + 1, y0 + 1);
     }
     return at((int)(u * (float)t.w), (int)(vv * (float)t.h));
+}
+
+// ------------------------------------------------------------------- SVNDF --
+// VonMisesFisherDistribution<4>::sample (VonMisesFisherDistribution.h:162-201) as
+// the reference draws it: lobe by the cumulative weights, tangential part in the
+// unit disk (r = sqrt(u)), W from the inverse CDF; L = 5 float4 (lobes, weights).
+__device__ __forceinline__ V3 vmf4SampleRef(const float4* L, Pcg& rng) {
+    const float4 al = __ldg(&L[4]);
+    const float u0 = rng.randf();
+    int k = 0;
+    float acc = al.x;
+    if (!(u0 <= acc)) { k = 1; acc += al.y; if (!(u0 <= acc)) { k = 2; acc += al.z; if (!(u0 <= acc)) k = 3; } }
+    const float4 l = __ldg(&L[k]);
+    const V3 mu(l.x, l.y, l.z);
+    const float kappa = l.w;
+    if (mu.x == 0.0f && mu.y == 0.0f && mu.z == 0.0f) return V3(0.0f, 0.0f, 0.0f);
+    const float u = rng.randf();
+    const float v = rng.randf();
+    const float r = sqrtf(u);
+    const float theta = (float)((double)(2.0f * kPi * v) - kPiD);
+    const float vx = r * cosf(theta), vy = r * sinf(theta);
+    const float u2 = rng.randf();
+    const float W = kappa > 0.0f ? 1.0f + powf(kappa, -1.0f) * logf(u2 + (1.0f - u2) * expf(-2.0f * kappa)) : 1.0f;
+    const float sq = safeSqrt(1.0f - powf(W, 2.0f));
+    Basis basis(normalize(mu));
+    return normalize(basis.toGlobal(W, sq * vx, sq * vy));
+}
+// SVNDF::sampleNormal (Prefiltering sandbox Main.cpp:366-388): a stochastic
+// bilinear choice of the texel (indices truncated, the y1 wrap compared with
+// resolutionU as in the reference, then kept inside the rows that exist).
+__device__ __forceinline__ V3 svndfSampleNormal(const SvndfDev& d, float2 uv, Pcg& rng) {
+    const float nu = uv.x - floorf(uv.x), nv = uv.y - floorf(uv.y);
+    int x0 = (int)(nu * (float)d.resU - 0.5f);
+    int y0 = (int)(nv * (float)d.resV - 0.5f);
+    int x1 = x0 + 1, y1 = y0 + 1;
+    const float wx1 = (nu * (float)d.resU - 0.5f) - (float)x0;
+    const float wy1 = (nv * (float)d.resV - 0.5f) - (float)y0;
+    if (x0 < 0) x0 = d.resU - 1;
+    if (y0 < 0) y0 = d.resV - 1;
+    if (x1 >= d.resU) x1 = 0;
+    if (y1 >= d.resU) y1 = 0;
+    if (y1 >= d.resV) y1 = 0;
+    x0 = min(max(x0, 0), d.resU - 1);
+    y0 = min(max(y0, 0), d.resV - 1);
+    const int x = (rng.randf() <= wx1) ? x1 : x0;
+    const int y = (rng.randf() <= wy1) ? y1 : y0;
+    return vmf4SampleRef(d.lobes + ((size_t)y * d.resU + x) * 5, rng);
 }
 
 // ------------------------------------------------------------------- skies --
@@ -339,7 +389,17 @@ __device__ __forceinline__ float G1m(V3 w, V3 wm, V3 wp, V3 wt, V3 wg) {
     return dot(w, wm) > 0.0f ? minf_ref(1.0f, clampPositive(dot(w, wg)) / (a_p(w, wp, wg) + a_t(w, wp, wt, wg))) : 0.0f;
 }
 
+// MultiLobeSVBRDF::perturbInteraction (Prefiltering sandbox Main.cpp:502-515).
+__device__ __forceinline__ Surface svbrdfPerturb(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng) {
+    Surface p = s;
+    const V3 n = svndfSampleNormal(sc.svndfs[m.tex], s.uv, rng);
+    p.sn = normalize(n.z * s.n + n.x * s.stan + n.y * s.sbit);
+    return p;
+}
+
 __device__ __forceinline__ V3 bsdfCos(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
+    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:489-491
+        return bsdfCosBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), wi);
     if (m.kind != MAT_MF_NORMALMAP) return bsdfCosBasic(sc, m, s, wi);
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:94-171
@@ -367,6 +427,8 @@ __device__ __forceinline__ V3 bsdfCos(const SceneDev& sc, const Material& m, con
 }
 
 __device__ __forceinline__ float getPDF(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:497-499, divided by the double M_PI
+        return (float)((double)clampPositive(dot(s.sn, wi)) / kPiD);
     if (m.kind != MAT_MF_NORMALMAP) return pdfBasic(sc, m, s, wi);
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:254-321
@@ -394,6 +456,8 @@ __device__ __forceinline__ float getPDF(const SceneDev& sc, const Material& m, c
 // *pdf is left untouched where the reference leaves it untouched.
 __device__ __forceinline__ V3 evalAndSample(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
                                             float* pdf) {
+    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:493-495
+        return sampleBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), rng, wi, pdf);
     if (m.kind != MAT_MF_NORMALMAP) return sampleBasic(sc, m, s, rng, wi, pdf);
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:173-252
@@ -437,6 +501,23 @@ __device__ __forceinline__ V3 albedoOf(const SceneDev& sc, const Material& m, co
     }
 }
 
+// Dispatch for the shade kernel: NESTED = false compiles only the materials that
+// evaluate no other material (scenes without microfacet normal mapping or
+// MultiLobeSVBRDF), which keeps the common kernel smaller.
+template <bool NESTED>
+__device__ __forceinline__ V3 bsdfCosT(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
+    return NESTED ? bsdfCos(sc, m, s, rng, wi) : bsdfCosBasic(sc, m, s, wi);
+}
+template <bool NESTED>
+__device__ __forceinline__ float getPDFT(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    return NESTED ? getPDF(sc, m, s, wi) : pdfBasic(sc, m, s, wi);
+}
+template <bool NESTED>
+__device__ __forceinline__ V3 evalAndSampleT(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
+                                             float* pdf) {
+    return NESTED ? evalAndSample(sc, m, s, rng, wi, pdf) : sampleBasic(sc, m, s, rng, wi, pdf);
+}
+
 // SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).
 __device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instance& in, int prim, float b0, float b1,
                                                V3 dWorld) {
@@ -457,6 +538,7 @@ __device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instanc
         s.stan = V3();
         s.sbit = V3();
     }
+    const V3 tanObj = s.stan, bitObj = s.sbit;  // isect.tangent / bitangent before any shading change
     s.sn = faceForward(s.sn, s.wo);
     if (m.shellLayers) {  // TriangleIndexedWithShellMapping::perturbIntersection (TriangleIndexed.h:237-254)
         const TextureDev d{m.shellTexels, m.shellW, m.shellH, m.shellClamp, m.shellFilter};
@@ -474,6 +556,10 @@ __device__ __forceinline__ Surface makeSurface(const SceneDev& sc, const Instanc
     if (mat.normalmap >= 0) {
         V3 nm = texLookup(sc.textures[mat.normalmap], s.uv.x, s.uv.y) * 2.0f - V3(1.0f);
         s.sn = normalize(nm.z * s.sn + nm.x * s.stan + nm.y * s.sbit);
+    }
+    if (mat.kind == MAT_MULTILOBE_SVBRDF) {  // isect.tangent / bitangent to world space (Object.h:52-57)
+        s.stan = isZero(tanObj) ? tanObj : (in.identity ? normalize(tanObj) : xformNormal(in.mat, tanObj));
+        s.sbit = isZero(bitObj) ? bitObj : (in.identity ? normalize(bitObj) : xformNormal(in.mat, bitObj));
     }
     s.sn = in.identity ? normalize(s.sn) : xformNormal(in.mat, s.sn);
     return s;

@@ -37,6 +37,11 @@ struct BlasBuildOutput {
 // Returns a CUDA error code (cudaSuccess on success).
 cudaError_t buildBlas(const BlasBuildInput& in, BlasBuildOutput* out, cudaStream_t stream);
 
+// SVNDF fit of a displacement map (svndf.cu): lobes [resV][resU][5] float4, low
+// heights [resV][resU] float4 (red channel). rate in [1, 16].
+cudaError_t svndfFit(const TextureDev& src, float scale, int rate, uint32_t seed, int resU, int resV, float4* lobes,
+                     float4* low, cudaStream_t s);
+
 // ---- wavefront (integrator.cu / trace.cu) --------------------------------------
 struct Ctrl {
     unsigned long long nextPath;   // next camera path id to generate
@@ -134,7 +139,8 @@ struct BatchView {
     const RenderParams* params;
     const unsigned long long* start;  // nJobs + 1 prefix sums of the jobs' path counts
     int nJobs;
-    int flat;  // every scene has <= 16 instances and binary mesh BVHs: the persistent per-lane kernels
+    int flat;    // every scene has <= 16 instances and binary mesh BVHs: the persistent per-lane kernels
+    int nested;  // some scene has a material that evaluates another (the shade kernel with that code)
 };
 void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
 void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,

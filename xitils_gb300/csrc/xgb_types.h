@@ -102,6 +102,7 @@ enum MaterialKind : int {
     MAT_SPECULAR_REFRACTION = 7,
     MAT_SPECULAR_FRESNEL = 8,
     MAT_MF_NORMALMAP = 9,
+    MAT_MULTILOBE_SVBRDF = 10,  // base material + SVNDF (index in `tex`)
 };
 
 struct __align__(16) Material {
@@ -126,6 +127,14 @@ struct TextureDev {
     int filter;  // Texture::filter
 };
 
+// SVNDF of a displacement map: per low texel 4 lobes as (mu.xyz, kappa) then the
+// 4 weights, 5 float4 per texel, row-major [resV][resU].
+constexpr int kSvndfLobes = 4;
+struct SvndfDev {
+    const float4* lobes;
+    int resU, resV;
+};
+
 enum SkyKind : int { SKY_NONE = 0, SKY_UNIFORM = 1, SKY_PROBE = 2, SKY_LATLONG = 3 };
 
 // One emissive object (Scene.h:17-22). Light triangle t of light L lives at
@@ -146,9 +155,11 @@ struct SceneDev {
     int blasLayout;  // every mesh binary (0), every mesh wide (1), or a mix (2)
     int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
     int shell;       // 1 when some mesh is shell-mapped (its hits can be discarded during traversal)
+    int nested;      // 1 when a material evaluates another (microfacet normal mapping, MultiLobeSVBRDF)
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;
+    const SvndfDev* svndfs;
     const LightDev* lights;
     int nLights;
     // per light triangle (world data precomputed with the reference's arithmetic):

@@ -20,6 +20,7 @@ from .transform import Transform
 # Material kinds (same numbering as the C ABI's xgb_material_kind).
 DIFFUSE, METAL, GLOSSY, GLOSSY_HIGHLIGHT, GLOSSY_CLAMPED, EMISSION = 0, 1, 2, 3, 4, 5
 SPECULAR_REFLECTION, SPECULAR_REFRACTION, SPECULAR_FRESNEL, MF_NORMALMAP = 6, 7, 8, 9
+MULTILOBE_SVBRDF = 10  # base material + SVNDF (the displacement sandbox's MultiLobeSVBRDF)
 # Sky kinds.
 SKY_NONE, SKY_UNIFORM, SKY_PROBE, SKY_LATLONG = 0, 1, 2, 3
 # Integrators.
@@ -28,9 +29,10 @@ STANDARD, NAIVE = 0, 1
 
 @dataclass
 class TextureDesc:
-    rgb: np.ndarray  # float32 [h, w, 3]
+    rgb: Optional[np.ndarray]  # float32 [h, w, 3]; None for the low-resolution texture of an SVNDF
     clamp: bool = True
     filter: bool = True
+    svndf: Optional[tuple] = None  # (source texture, displacement scale, rate, seed) of a derived texture
 
 
 @dataclass
@@ -90,6 +92,7 @@ class SceneDesc:
     spp: int = 1
     params: IntegratorParams = field(default_factory=IntegratorParams)
     fixes: int = 0  # opt-in quirk fixes of the render (2 = drop non-finite contributions)
+    svndf_count: int = 0
 
     # -- construction -----------------------------------------------------
     def add_texture(self, rgb: np.ndarray, clamp: bool = True, filter: bool = True) -> int:
@@ -114,6 +117,16 @@ class SceneDesc:
         assert all(a is not None for a in (m.uv, m.nrm, m.tan, m.bit)), "shell mapping needs every attribute"
         m.shell = (int(displacement), float(scale), int(layers))
         return i
+
+    def add_svndf(self, displacement: int, scale: float, rate: int = 8, seed: int = 0):
+        """SVNDF of a displacement texture (the displacement sandbox's
+        downsampleDisplacementTexture): per rate x rate block a 4-lobe vMF fit of the
+        block's normals and the block's mean height. Returns (svndf id, id of the
+        low-resolution height texture, which is added to the textures)."""
+        src = self.textures[displacement]
+        self.textures.append(TextureDesc(None, src.clamp, True, (int(displacement), float(scale), int(rate), int(seed))))
+        self.svndf_count += 1
+        return self.svndf_count - 1, len(self.textures) - 1
 
     def add_material(self, kind: int, f=(), base: int = -1, tex: int = -1, normalmap: int = -1) -> int:
         self.materials.append(MaterialDesc(kind, [float(x) for x in f], base, tex, normalmap))
@@ -169,7 +182,10 @@ class SceneDesc:
         add_object / set_camera / set_sky / build (see xitils_gb300.api.Scene and
         the CPU checker bindings)."""
         for t in self.textures:
-            backend.add_texture(t.rgb, t.clamp, t.filter)
+            if t.svndf is not None:
+                backend.add_svndf(*t.svndf)
+            else:
+                backend.add_texture(t.rgb, t.clamp, t.filter)
         for m in self.meshes:
             if m.shell:
                 backend.add_mesh_shell(m.pos, m.idx, m.uv, m.nrm, m.tan, m.bit, *m.shell)

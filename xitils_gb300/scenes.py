@@ -440,14 +440,19 @@ def weave_displacement(res: int = 256, threads: int = 8) -> np.ndarray:
 
 def shell_fabric(width: int = 512, height: int = 512, spp: int = 16, grid: int = 96, layers: int = 16,
                  disp_scale: float = 0.012, tiling: float = 6.0, tex_res: int = 256, max_depth: int = 0,
-                 seed: int = 5) -> SceneDesc:
+                 seed: int = 5, method: str = "shell", rate: int = 8) -> SceneDesc:
     """Displacement-mapped fabric by shell mapping, after the reference's
     displacement sandbox (a cloth under GlossyWithHighLight((0.8, 0.2, 0.2), 1, 2,
     10, 0.05) with 16 shell layers in a Cornell-style room lit from the ceiling):
     a draped grid x grid cloth patch whose texcoords tile a plain-weave height map
     `tiling` times, layers copies up to disp_scale along the normals, inside a
     unit room with a 0.4 x 0.4 ceiling light. Reference integrator defaults
-    (no depth limit, Russian roulette after 5 at 0.9) unless max_depth is set."""
+    (no depth limit, Russian roulette after 5 at 0.9) unless max_depth is set.
+
+    method = "svbrdf" is the sandbox's naive prefiltering (MethodModeMultiLobeSVBRDF):
+    the displacement map is downsampled by `rate` with a 4-lobe vMF SVNDF fitted per
+    low texel, the shells follow the low-resolution map and the material is
+    MultiLobeSVBRDF(base, low map, scale, SVNDF)."""
     from .scene import GLOSSY_HIGHLIGHT
     s = SceneDesc(name="shell_fabric", width=width, height=height, spp=spp,
                   params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed))
@@ -477,7 +482,14 @@ def shell_fabric(width: int = 512, height: int = 512, spp: int = 16, grid: int =
     pos[:, 2] = 0.1 + 0.8 * pos[:, 2]
     nrm, tan, bit = heightfield_frames(heights * F(1.0 / 0.8), extent=1.0)
     disp = s.add_texture(weave_displacement(tex_res), clamp=False, filter=True)
-    cloth = s.add_mesh_shell(pos, idx, uv * F(tiling), nrm, tan, bit, disp, disp_scale, layers)
-    s.add_object(cloth, s.add_material(GLOSSY_HIGHLIGHT, [0.8, 0.2, 0.2, 1.0, 1.0, 1.0, 2.0, 10.0, 0.05]))
+    base = s.add_material(GLOSSY_HIGHLIGHT, [0.8, 0.2, 0.2, 1.0, 1.0, 1.0, 2.0, 10.0, 0.05])
+    if method == "svbrdf":
+        from .scene import MULTILOBE_SVBRDF
+        svndf, low = s.add_svndf(disp, disp_scale, rate, seed)
+        cloth = s.add_mesh_shell(pos, idx, uv * F(tiling), nrm, tan, bit, low, disp_scale, layers)
+        s.add_object(cloth, s.add_material(MULTILOBE_SVBRDF, [], base=base, tex=svndf))
+    else:
+        cloth = s.add_mesh_shell(pos, idx, uv * F(tiling), nrm, tan, bit, disp, disp_scale, layers)
+        s.add_object(cloth, base)
     s.set_camera(look_at((0.5, 0.55, -0.35), (0.5, 0.08, 0.5), (0, 1, 0)), 40.0 * math.pi / 180.0, height / width)
     return s
