@@ -119,7 +119,7 @@ def make_workload(args):
         desc = scenes.cornell(res, res, spp)
         label = f"cornell 36 tris, {res}x{res} film, {spp} spp, max depth 8, RR after depth 3"
         meta = {"data": "synthetic (the Cornell box of the workload description)", "kernel": SINGLE_KERNEL,
-                "l2": "the scene fits in L2 (36 triangles); path queues of 2^21 paths stream through HBM"}
+                "l2": "the scene fits in L2 (36 triangles); path queues of 2^23 paths stream through HBM"}
     return desc, label, meta
 
 
@@ -537,7 +537,7 @@ def run_xgb(args):
         "data": meta["data"],
         "config": {"workload": label, "parallelism": f"replicas x{world} (disjoint sample ranges)",
                    "l2": meta["l2"],
-                   "queue_capacity": 1 << 21},
+                   "queue_capacity": 1 << 23},
         "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC),
                 "d2h_bytes_per_step": W * H * 12},
         "gpu_launches": agg["kernel_launches"] // len(stats) * args.steps,

@@ -248,7 +248,7 @@ typedef struct {
     int rr_start;     /* Russian roulette when pathLength > rr_start (reference: 5) */
     float rr_prob;    /* survival probability (reference: 0.9) */
     uint32_t seed;    /* PCG stream seed: stream(pixel, sample) = pcg32(splitmix64(seed<<32 ^ sample), pixel) */
-    int queue_capacity; /* paths in flight, 0 = automatic */
+    int queue_capacity; /* paths in flight, 0 = automatic (2^23, or the call's path count if smaller) */
 } xgb_integrator_params;
 
 /* Fills the reference's defaults (PathTracer.h:253-257). */
@@ -305,7 +305,7 @@ typedef struct {
  * sample counts; the first call of a new shape runs the autotuner) with graphs. */
 xgb_status xgb_render_batch(const xgb_batch_job* jobs, int n, const xgb_batch_options* options, void* stream);
 /* Times short trial renders (1 sample per pixel of every job, into scratch films)
- * for queue capacities 2^18 .. 2^21 and 4 / 8 / 16 iterations per check; writes
+ * for queue capacities 2^18 .. 2^23 and 4 / 8 / 16 iterations per check; writes
  * the fastest to *out and caches it for this batch shape. */
 xgb_status xgb_batch_autotune(const xgb_batch_job* jobs, int n, void* stream, xgb_batch_options* out);
 /* Counters of the last xgb_render_batch of this context. */

@@ -210,6 +210,23 @@ class Context:
             pass
 
 
+def _release(obj, destroy: str) -> None:
+    """Destroys obj's handle while its context is alive. Every wrapper keeps Python
+    references to the handles its handle points at (a scene to its meshes, materials,
+    textures and guide; a material to its textures, base and SVNDF; a shell-mapped
+    mesh to its displacement map), so nothing the library still reads is freed; the
+    library's destroy calls free device memory with cudaFree, which waits for the
+    device's work in flight."""
+    h = getattr(obj, "h", None)
+    ctx = getattr(obj, "ctx", None)
+    if h and ctx is not None and getattr(ctx, "h", None):
+        try:
+            getattr(ctx.lib, destroy)(h)
+        except Exception:
+            pass
+    obj.h = None
+
+
 class Texture:
     """xitils::Texture built from float RGB texels [h, w, 3] (Texture.h:25-32)."""
 
@@ -220,6 +237,9 @@ class Texture:
         self.h = P()
         ctx.check(ctx.lib.xgb_texture_create(ctx.h, w, h, ch, _fp(rgb), int(warpClamp), int(filter), C.byref(self.h)),
                   "Texture")
+
+    def __del__(self):
+        _release(self, "xgb_texture_destroy")
 
 
 class Svndf:
@@ -248,6 +268,9 @@ class Svndf:
     def set_lobes(self, lobes: np.ndarray):
         lobes = _f32(lobes).reshape(self.height, self.width, 4, 5)
         self.ctx.check(self.ctx.lib.xgb_svndf_set_lobes(self.h, _fp(lobes)), "Svndf.set_lobes")
+
+    def __del__(self):
+        _release(self, "xgb_svndf_destroy")
 
 
 class TriangleMesh:
@@ -290,6 +313,9 @@ class TriangleMesh:
         self.n_tris = idx.size // 3 * int(layerNum)
         return self
 
+    def __del__(self):
+        _release(self, "xgb_mesh_destroy")
+
 
 class Material:
     def __init__(self, ctx: Context, maker, *args):
@@ -302,11 +328,15 @@ class Material:
         self.normalmap = tex
         self.ctx.check(self.ctx.lib.xgb_material_set_normalmap(self.h, tex.h if tex else None), "normalmap")
 
+    def __del__(self):
+        _release(self, "xgb_material_destroy")
+
 
 class Diffuse(Material):
     def __init__(self, ctx, albedo, texture: Optional[Texture] = None):
         a = _f32(albedo, 3)
         super().__init__(ctx, ctx.lib.xgb_material_diffuse, _fp(a), texture.h if texture else None)
+        self.texture = texture
 
 
 class Metal(Material):
@@ -314,6 +344,7 @@ class Metal(Material):
         f = _f32(f0, 3)
         super().__init__(ctx, ctx.lib.xgb_material_metal, C.c_float(roughness), _fp(f),
                          roughness_texture.h if roughness_texture else None)
+        self.roughness_texture = roughness_texture
 
 
 class Glossy(Material):
@@ -421,6 +452,9 @@ class Scene:
     def buildAccelerationStructure(self, stream=None):
         self.ctx.check(self.ctx.lib.xgb_scene_build(self.h, stream), "buildAccelerationStructure")
 
+    def __del__(self):
+        _release(self, "xgb_scene_destroy")
+
     def setGuide(self, guide, bsdf_fraction: float = 0.5, train: bool = False, lr: float = 1e-3):
         self.ctx.check(self.ctx.lib.xgb_scene_set_guide(self.h, guide.h if guide else None, C.c_float(bsdf_fraction),
                                                         int(train), C.c_float(lr)), "setGuide")
@@ -467,6 +501,9 @@ class RenderTarget:
         ctx.check(ctx.lib.xgb_film_create(ctx.h, width, height, int(fp64), C.byref(self.h)), "RenderTarget")
         if aovs:
             ctx.check(ctx.lib.xgb_film_enable_aovs(self.h), "enable_aovs")
+
+    def __del__(self):
+        _release(self, "xgb_film_destroy")
 
     def tonemap(self, scale: float = 1.0, exposure: float = 0.3, gamma: float = 2.2, stream=None) -> np.ndarray:
         """8-bit display image [H, W, 3] (RTCamp8's mapping; scale = 1 / spp)."""
@@ -574,6 +611,9 @@ class Guide:
         n = C.c_size_t()
         ctx.lib.xgb_guide_param_count(C.byref(n))
         self.n_params = n.value
+
+    def __del__(self):
+        _release(self, "xgb_guide_destroy")
 
     def params(self) -> np.ndarray:
         out = np.empty(self.n_params, np.float32)

@@ -1214,7 +1214,9 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     s->last = xgb_render_stats{};
     unsigned long long total = (unsigned long long)film->w * film->h * spp_count;
     if (total == 0) return XGB_OK;
-    unsigned int cap = P.queue_capacity > 0 ? (unsigned int)P.queue_capacity : (1u << 21);
+    // 2^23 paths in flight (~1.7 GB of queues) by default: on the terrain 2^21 -> 2^22 -> 2^23
+    // gave 1162 -> 1280 -> 1346 Mpaths/s (fewer, fuller wavefront launches)
+    unsigned int cap = P.queue_capacity > 0 ? (unsigned int)P.queue_capacity : (1u << 23);
     if ((unsigned long long)cap > total) cap = (unsigned int)std::max<unsigned long long>(total, 1024ull);
     cap = (cap + 255u) & ~255u;
     xgb_status bs = ensureBuffers(s, cap);

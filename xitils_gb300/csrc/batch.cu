@@ -333,7 +333,7 @@ xgb_status xgb_batch_autotune(const xgb_batch_job* jobs, int n, void* stream, xg
     xgb_batch_options best{1 << 20, 8, 1};
     double bestT = 1e30;
     if (st2 == XGB_OK) {
-        const unsigned int caps[] = {1u << 18, 1u << 19, 1u << 20, 1u << 21};
+        const unsigned int caps[] = {1u << 18, 1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23};
         for (unsigned int cap : caps) {
             xgb_batch_options o{(int)cap, 8, 1};
             double t = 0;
