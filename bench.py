@@ -50,10 +50,10 @@ L2_BYTES = 129 * 1024 * 1024
 EXTEND_BYTES_PER_RAY = 52
 # BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
 NODE_BYTES, TRI_BYTES = 64, 48
-# DRAM bytes per extension ray of k_extend from one ncu capture on this scene
-# (profiles/extend_terrain_ncu_full.md: ~600 MB per ~2.03 M rays, 512x512x16 case,
-# same 2.09 M-triangle BVH); scaled to the average launch for roofline.traffic.
-EXTEND_DRAM_BYTES_PER_RAY = 295.0
+# DRAM bytes per extension ray of k_trace_single from one ncu capture of a full
+# 8,388,608-ray launch on the terrain (profiles/trace_single_terrain_ncu.md: 1.235 GB
+# read + 178.7 MB written); scaled to the average launch for roofline.traffic.
+EXTEND_DRAM_BYTES_PER_RAY = 168.5
 
 
 def parse():
@@ -518,7 +518,7 @@ def run_xgb(args):
         "unit": "GB/s",
         "frac": (achieved / (hbm or 6800.0)) if achieved else None,
         "traffic": EXTEND_DRAM_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
-        "traffic_source": "ncu dram__bytes_read+write per ray (profiles/extend_terrain_ncu_full.md) x rays per launch",
+        "traffic_source": "ncu dram__bytes_read+write per ray (profiles/trace_single_terrain_ncu.md) x rays per launch",
         "algorithmic_bytes_per_launch": EXTEND_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
         "avg_launch_ms": ext_ms / ext_launches,
         "bvh_l2_gbs": ((NODE_BYTES * agg["node_visits"] + TRI_BYTES * agg["tri_tests"]) / (ext_ms / 1e3) / 1e9
