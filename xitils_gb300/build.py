@@ -4,8 +4,8 @@ Each CUDA translation unit is compiled by nvcc in parallel with
 ``-gencode arch=compute_103a,code=sm_103a`` and linked into the in-tree shared
 library ``xitils_gb300/libxgb.so`` (CUDA runtime linked statically; no PyTorch
 dependency). Per-unit flags:
-  * integrator.cu, svndf.cu: ``-fmad=false`` -- shading and fitting arithmetic
-    stays unfused, as in the reference's float code;
+  * integrator.cu, shade_*.cu, svndf.cu: ``-fmad=false``
+    -- shading and fitting arithmetic stays unfused, as in the reference's float code;
   * api.cu: host code compiled with ``-ffp-contract=off`` for the same reason.
 """
 from __future__ import annotations
@@ -30,6 +30,7 @@ UNITS = {
     "noalloc.cu": [],
     "guide.cu": [], "image.cu": [], "batch.cu": [],
     "svndf.cu": ["-fmad=false"],
+    "shade_layered.cu": ["-fmad=false"], "shade_nested.cu": ["-fmad=false"], "shade_batch_nested.cu": ["-fmad=false"],
 }
 
 

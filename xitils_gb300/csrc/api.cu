@@ -1049,7 +1049,7 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.fixes = (int)s->fixes;
     sd.shell = anyShell;
     sd.nested = 0;
-    for (const Material& m : dm) sd.nested |= (m.kind == MAT_MF_NORMALMAP || m.kind == MAT_MULTILOBE_SVBRDF) ? 1 : 0;
+    for (const Material& m : dm) sd.nested |= (m.kind == MAT_MF_NORMALMAP ? 1 : 0) | (m.kind == MAT_MULTILOBE_SVBRDF ? 2 : 0);
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;

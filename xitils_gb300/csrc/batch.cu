@@ -174,7 +174,7 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
         SceneDev sd; int dev, sms, built; cudaStream_t cs;
         sceneView(jobs[i].scene, &sd, &dev, &sms, &cs, &built);
         if (sd.nInstances > 16 || sd.blasLayout != 0 || sd.shell) flat = 0;
-        nested |= sd.nested;
+        nested |= sd.nested ? 1 : 0;
         void* fd; int w, h, f64, fdev; cudaStream_t fcs;
         filmPlane(jobs[i].film, &fd, &w, &h, &f64, &fdev, &fcs);
         const xgb_integrator_params& P = jobs[i].params;

@@ -397,10 +397,8 @@ __device__ __forceinline__ Surface svbrdfPerturb(const SceneDev& sc, const Mater
     return p;
 }
 
-__device__ __forceinline__ V3 bsdfCos(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
-    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:489-491
-        return bsdfCosBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), wi);
-    if (m.kind != MAT_MF_NORMALMAP) return bsdfCosBasic(sc, m, s, wi);
+// MicrofacetNormalMapping (m.kind == MAT_MF_NORMALMAP) bsdfCos / getPDF / evalAndSample.
+__device__ __forceinline__ V3 bsdfCosMfnm(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:94-171
     if (f.kind == 0) return bsdfCosBasic(sc, b, s, wi);
@@ -426,10 +424,7 @@ __device__ __forceinline__ V3 bsdfCos(const SceneDev& sc, const Material& m, con
     return result;
 }
 
-__device__ __forceinline__ float getPDF(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
-    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:497-499, divided by the double M_PI
-        return (float)((double)clampPositive(dot(s.sn, wi)) / kPiD);
-    if (m.kind != MAT_MF_NORMALMAP) return pdfBasic(sc, m, s, wi);
+__device__ __forceinline__ float getPDFMfnm(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:254-321
     if (f.kind == 0) return pdfBasic(sc, b, s, wi);
@@ -452,13 +447,8 @@ __device__ __forceinline__ float getPDF(const SceneDev& sc, const Material& m, c
     return pdf + diff * clampPositive(dot(wi, f.wg)) / kPi;
 }
 
-// Returns material_eval = f * cos / pdf and samples wi (Material.h:22-28).
-// *pdf is left untouched where the reference leaves it untouched.
-__device__ __forceinline__ V3 evalAndSample(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
-                                            float* pdf) {
-    if (m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:493-495
-        return sampleBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), rng, wi, pdf);
-    if (m.kind != MAT_MF_NORMALMAP) return sampleBasic(sc, m, s, rng, wi, pdf);
+__device__ __forceinline__ V3 evalAndSampleMfnm(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng,
+                                                V3* wi, float* pdf) {
     const Material& b = sc.materials[m.base];
     MfnmFrame f = mfnmFrame(s);  // Main.cpp:173-252
     if (f.kind == 0) return sampleBasic(sc, b, s, rng, wi, pdf);
@@ -483,7 +473,7 @@ __device__ __forceinline__ V3 evalAndSample(const SceneDev& sc, const Material& 
         if (i > 100) { weight = weight * V3(0.0f); break; }
     }
     *wi = wr;
-    *pdf = !specular ? getPDF(sc, m, s, *wi) : -1.0f;
+    *pdf = !specular ? getPDFMfnm(sc, m, s, *wi) : -1.0f;
     return V3(0.0f) + weight;
 }
 
@@ -501,21 +491,33 @@ __device__ __forceinline__ V3 albedoOf(const SceneDev& sc, const Material& m, co
     }
 }
 
-// Dispatch for the shade kernel: NESTED = false compiles only the materials that
-// evaluate no other material (scenes without microfacet normal mapping or
-// MultiLobeSVBRDF), which keeps the common kernel smaller.
-template <bool NESTED>
+// Material dispatch (Material.h:9-48). NESTED is a mask of the materials that
+// evaluate another material which the code is compiled for: 1 microfacet normal
+// mapping, 2 MultiLobeSVBRDF. The shade kernel is instantiated per mask so that a
+// scene only carries the code (and registers) of the materials it has.
+template <int NESTED>
 __device__ __forceinline__ V3 bsdfCosT(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
-    return NESTED ? bsdfCos(sc, m, s, rng, wi) : bsdfCosBasic(sc, m, s, wi);
+    if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:489-491
+        return bsdfCosBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), wi);
+    if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return bsdfCosMfnm(sc, m, s, rng, wi);
+    return bsdfCosBasic(sc, m, s, wi);
 }
-template <bool NESTED>
+template <int NESTED>
 __device__ __forceinline__ float getPDFT(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
-    return NESTED ? getPDF(sc, m, s, wi) : pdfBasic(sc, m, s, wi);
+    if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:497-499, divided by the double M_PI
+        return (float)((double)clampPositive(dot(s.sn, wi)) / kPiD);
+    if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return getPDFMfnm(sc, m, s, wi);
+    return pdfBasic(sc, m, s, wi);
 }
-template <bool NESTED>
+// Returns material_eval = f * cos / pdf and samples wi (Material.h:22-28).
+// *pdf is left untouched where the reference leaves it untouched.
+template <int NESTED>
 __device__ __forceinline__ V3 evalAndSampleT(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
                                              float* pdf) {
-    return NESTED ? evalAndSample(sc, m, s, rng, wi, pdf) : sampleBasic(sc, m, s, rng, wi, pdf);
+    if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:493-495
+        return sampleBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), rng, wi, pdf);
+    if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return evalAndSampleMfnm(sc, m, s, rng, wi, pdf);
+    return sampleBasic(sc, m, s, rng, wi, pdf);
 }
 
 // SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).

@@ -155,7 +155,7 @@ struct SceneDev {
     int blasLayout;  // every mesh binary (0), every mesh wide (1), or a mix (2)
     int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
     int shell;       // 1 when some mesh is shell-mapped (its hits can be discarded during traversal)
-    int nested;      // 1 when a material evaluates another (microfacet normal mapping, MultiLobeSVBRDF)
+    int nested;      // materials that evaluate another: bit 0 microfacet normal mapping, bit 1 MultiLobeSVBRDF
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;

@@ -387,8 +387,12 @@ def mfnm_at_scale(width: int = 2048, height: int = 2048, spp: int = 256, grid: i
     roughness is uniform per texel in [0.1, 0.4], with a normal_res^2 normal map from fBm gradients (slope scale
     1.5); lit by the procedural lat-long environment plus 2 quad lights.
     Reference Russian roulette (after 5 at 0.9) and max depth 12."""
+    # 2^21 paths in flight: the normal-mapping walk re-reads the 2048^2 normal map at
+    # every facet bounce, and a smaller queue streams less past it through L2
+    # (95 against 91 Mpaths/s with the default 2^23)
     s = SceneDesc(name="mfnm_at_scale", width=width, height=height, spp=spp,
-                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed))
+                  params=IntegratorParams(max_depth=max_depth, rr_start=5, rr_prob=0.9, seed=seed,
+                                          queue_capacity=1 << 21))
     rng = np.random.default_rng(seed)
     h = fbm_heights(grid, seed)
     pos, uv, idx = heightfield_mesh(h)
