@@ -323,7 +323,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
 // same closest-hit acceptance (tMax shrinks across instances).
 constexpr int kSentinel = 0x7FFFFFFF;
 
-template <bool ANY, bool COUNT, class S>
+// SHELL: the scene has shell-mapped meshes, whose accepted hits go through the
+// discard test (shellDiscard, trace.cuh) before tMax shrinks.
+template <bool ANY, bool COUNT, class S, bool SHELL = false>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue q, HitQueue h, ShadowQueue s,
                                                             PathQueue out, Ctrl* ctrl) {
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
@@ -342,6 +344,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
     WRay r;
     const Node2* nodes = nullptr;
     const TriV* tris = nullptr;
+    const MeshDev* mesh = nullptr;
     float tMax = 0.0f;
     TraceHit hit;
     hit.prim = -1;
@@ -406,6 +409,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             const MeshDev& m = sc.meshes[in.mesh];
             nodes = m.nodes2;
             tris = m.tris;
+            mesh = &m;
             if (in.identity) r = makeWRay(wo, wd);
             else r = makeWRay(xformPointRn(in.matInv, wo), xformVectorRn(in.matInv, wd));
             sp = 0;
@@ -450,6 +454,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
                 float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
                 float t, b0, b1;
                 if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
+                    if (SHELL && mesh->shellLayers && shellDiscard(*mesh, __float_as_int(p0.w), b0, b1)) continue;
                     tMax = t;
                     if (ANY) { occluded = true; break; }
                     hit.t = t; hit.b0 = b0; hit.b1 = b1;
@@ -707,16 +712,28 @@ static int persistentGrid(K kernel, int numSMs) {
     return numSMs * it->second;
 }
 
-// The specialised kernels (one instance, flat instance lists, wide BVHs) have no
-// shell-mapping discard; a scene with a shell-mapped mesh takes the generic pair.
+// Of the specialised kernels only the flat binary one carries the shell-mapping
+// discard (its SHELL variant, which also takes one-instance shell scenes); a scene
+// with a shell-mapped mesh otherwise takes the generic pair.
 void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, bool count, cudaStream_t s) {
     RenderParams none{};
-    const bool flat = sc.nInstances <= kFlatInstances && !sc.shell;
+    const bool flat = sc.nInstances <= kFlatInstances;
 #define XGB_LAUNCH(K) K<<<persistentGrid(K, numSMs), kTraceBlock, 0, s>>>
+    if (sc.shell) {
+        if (flat && sc.blasLayout == 0) {
+            if (count) XGB_LAUNCH((k_trace_flat2<false, true, OneScene, true>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+            else XGB_LAUNCH((k_trace_flat2<false, false, OneScene, true>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        } else if (count) {
+            XGB_LAUNCH((k_extend<true>))(sc, q, h, ctrl);
+        } else {
+            XGB_LAUNCH((k_extend<false>))(sc, q, h, ctrl);
+        }
+        return;
+    }
     if (flat && sc.blasLayout == 1) {
         if (count) XGB_LAUNCH((k_trace_wide<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_wide<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-    } else if (sc.nInstances == 1 && sc.blasLayout == 0 && !sc.shell) {
+    } else if (sc.nInstances == 1 && sc.blasLayout == 0) {
         if (count) XGB_LAUNCH((k_trace_single<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_single<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (flat && sc.blasLayout == 0) {
@@ -739,9 +756,15 @@ void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* 
 
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s) {
-    const bool flat = sc.nInstances <= kFlatInstances && !sc.shell;
+    const bool flat = sc.nInstances <= kFlatInstances;
+    if (sc.shell) {
+        if (flat && sc.blasLayout == 0)
+            XGB_LAUNCH((k_trace_flat2<true, false, OneScene, true>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);
+        else XGB_LAUNCH(k_shadow)(sc, rp, sq, out, ctrl);
+        return;
+    }
     if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
-    else if (sc.nInstances == 1 && sc.blasLayout == 0 && !sc.shell)
+    else if (sc.nInstances == 1 && sc.blasLayout == 0)
         XGB_LAUNCH((k_trace_single<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (flat && sc.blasLayout == 0)
         XGB_LAUNCH((k_trace_flat2<true, false, OneScene>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);
