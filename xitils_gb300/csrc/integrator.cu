@@ -85,7 +85,10 @@ void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQu
     case 1: launchShadeMask1(job, in, h, out, sq, ctrl, grid, s); break;
     case 2: launchShadeMask2(job, in, h, out, sq, ctrl, grid, s); break;
     case 3: launchShadeMask3(job, in, h, out, sq, ctrl, grid, s); break;
-    default: k_shade<OneJob, 0><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl); break;
+    default:
+        if (rp.guided || rp.train || rp.aov) k_shade<OneJob, 0, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+        else k_shade<OneJob, 0, false><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+        break;
     }
 }
 
@@ -97,7 +100,7 @@ void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue ou
                       cudaStream_t s) {
     const ManyJobs jobs{b.scenes, b.params, b.start, b.nJobs};
     if (b.nested) launchShadeMask3Batch(jobs, in, h, out, sq, ctrl, grid, s);
-    else k_shade<ManyJobs, 0><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+    else k_shade<ManyJobs, 0, false><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb

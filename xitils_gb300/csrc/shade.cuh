@@ -176,8 +176,14 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
     mx.lobe[4].alpha = a1.x; mx.lobe[5].alpha = a1.y; mx.lobe[6].alpha = a1.z; mx.lobe[7].alpha = a1.w;
 }
 
-template <class J, int NESTED>
-__global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
+// EXTRAS: the learned proposal (guided sampling, training records), AOV planes;
+// plain renders run the variant without that code (fewer registers, a smaller
+// instruction footprint). That variant is held to three blocks per SM (80
+// registers, ~80 bytes of spills): on the terrain its launches took 12.6 instead
+// of 15.0 ms per render at two blocks (104 registers, no spills), on the Cornell
+// box 2.03 instead of 1.98 ms.
+template <class J, int NESTED, bool EXTRAS>
+__global__ void __launch_bounds__(kShadeBlock, (EXTRAS || NESTED) ? 1 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
                                                        ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
     const int lane = threadIdx.x & 31;
@@ -209,8 +215,8 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
             V3 thr(t4.x, t4.y, t4.z);
             // guide training: the record of the vertex this ray left takes the
             // path's accumulated contribution now, before this vertex adds any
-            const unsigned int pid = rp.train ? in.pid[i] : 0u;
-            if (rp.train) {
+            const unsigned int pid = (EXTRAS && rp.train) ? in.pid[i] : 0u;
+            if (EXTRAS && rp.train) {
                 const int prevRec = in.grec[i];
                 if (prevRec >= 0) {
                     float4 a = rp.pathAcc[pid];
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
             V3 acc(0.0f);  // this vertex's contributions (training accumulator)
             auto contribute = [&](V3 c) {
                 filmAddS(rp, pix, c);
-                if (rp.train) acc = acc + c;
+                if (EXTRAS && rp.train) acc = acc + c;
             };
             Pcg rng;
             rng.state = ((uint64_t)rs.y << 32) | rs.x;
@@ -239,7 +245,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                 const Material& mat = sc.materials[inst.material];
                 Surface s = makeSurface(sc, inst, prim, h.y, h.z, dir);
                 const bool emissive = mat.kind == MAT_EMISSION;
-                if (rp.aov && (flags & FLAG_PRIMARY)) aovAdd(rp, pix, albedoOf(sc, mat, s), s.n);
+                if (EXTRAS && rp.aov && (flags & FLAG_PRIMARY)) aovAdd(rp, pix, albedoOf(sc, mat, s), s.n);
                 if (naive) {
                     // NaivePathTracer::eval (PathTracer.h:75-100): emission, BSDF sample,
                     // then the next loop top (depth limit, Russian roulette) before tracing.
@@ -300,7 +306,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                         V3 wi;
                         float pdf = pdfPrev;  // left untouched by materials that do not set it
                         V3 f;
-                        const bool guidedHere = rp.guided && guidable(sc, mat);
+                        const bool guidedHere = EXTRAS && rp.guided && guidable(sc, mat);
                         VmfMixture mx;
                         float fcos = 0.0f;  // luminance of bsdfCos(wi) at a guided vertex
                         if (!guidedHere) {
@@ -370,7 +376,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                             r.thr = make_float4(thrNext.x, thrNext.y, thrNext.z, __int_as_float(packed));
                             r.rng = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
                             cont = true;
-                            if (rp.train && guidedHere && pdf > 0.0f && keepRecord(pid, len, rp.recordProb)) {
+                            if (EXTRAS && rp.train && guidedHere && pdf > 0.0f && keepRecord(pid, len, rp.recordProb)) {
                                 unsigned int slot = atomicAdd(rp.arenaCount, 1u);
                                 if (slot < (unsigned int)rp.arenaCap) {
                                     GuideRecord g;
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
                     }
                 }
             }
-            if (rp.train && !isZero(acc)) {
+            if (EXTRAS && rp.train && !isZero(acc)) {
                 float4 a = rp.pathAcc[pid];
                 rp.pathAcc[pid] = make_float4(a.x + acc.x, a.y + acc.y, a.z + acc.z, a.w);
             }
@@ -407,7 +413,7 @@ __global__ void __launch_bounds__(kShadeBlock) k_shade(J jobs, PathQueue in, Hit
         if (lane == 0 && mc) oc = atomicAdd(&ctrl->nOut, (unsigned int)__popc(mc));
         oc = __shfl_sync(kFull, oc, 0);
         unsigned int slot = oc + __popc(mc & ((1u << lane) - 1u));
-        const bool train = jobs.params(0).train;  // guide training runs with one job only
+        const bool train = EXTRAS && jobs.params(0).train;  // guide training runs with one job only
         if (cont) {
             out.o[slot] = r.o;
             out.d[slot] = r.d;

@@ -1,12 +1,13 @@
 // Shade kernel variant with both nested materials (mask 3) for the batches that
-// contain any nested material; see shade.cuh. Compiled with -fmad=false.
+// contain any nested material (batches take neither guiding nor AOV planes); see
+// shade.cuh. Compiled with -fmad=false.
 #include "shade.cuh"
 
 namespace xgb {
 
 void launchShadeMask3Batch(const ManyJobs& jobs, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
                            int grid, cudaStream_t s) {
-    k_shade<ManyJobs, 3><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+    k_shade<ManyJobs, 3, false><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb

@@ -6,12 +6,12 @@ namespace xgb {
 
 void launchShadeMask1(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
                       cudaStream_t s) {
-    k_shade<OneJob, 1><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    k_shade<OneJob, 1, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
 }
 
 void launchShadeMask2(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
                       cudaStream_t s) {
-    k_shade<OneJob, 2><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    k_shade<OneJob, 2, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb

@@ -6,7 +6,7 @@ namespace xgb {
 
 void launchShadeMask3(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
                       cudaStream_t s) {
-    k_shade<OneJob, 3><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    k_shade<OneJob, 3, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
 }
 
 }  // namespace xgb
