@@ -178,12 +178,14 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
 
 // EXTRAS: the learned proposal (guided sampling, training records), AOV planes;
 // plain renders run the variant without that code (fewer registers, a smaller
-// instruction footprint). That variant is held to three blocks per SM (80
-// registers, ~80 bytes of spills): on the terrain its launches took 12.6 instead
-// of 15.0 ms per render at two blocks (104 registers, no spills), on the Cornell
-// box 2.03 instead of 1.98 ms.
+// instruction footprint). Occupancy bounds, measured on GB300: without nested
+// materials three blocks per SM (80 registers, ~80 bytes of spills) -- terrain
+// shading 12.6 instead of 15.0 ms per render at two blocks, the guided room 82.5
+// instead of 79.9 Mpaths/s, the Cornell box 2.03 instead of 1.98 ms; with nested
+// materials two blocks (128 registers, 60-90 bytes of spills) -- the
+// normal-mapping scene 101 instead of 88 Mpaths/s at one block (140 registers).
 template <class J, int NESTED, bool EXTRAS>
-__global__ void __launch_bounds__(kShadeBlock, (EXTRAS || NESTED) ? 1 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
+__global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
                                                        ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
     const int lane = threadIdx.x & 31;
