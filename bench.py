@@ -51,9 +51,9 @@ EXTEND_BYTES_PER_RAY = 52
 # BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
 NODE_BYTES, TRI_BYTES = 64, 48
 # DRAM bytes per extension ray of k_trace_single from one ncu capture of a full
-# 8,388,608-ray launch on the terrain (profiles/trace_single_terrain_ncu.md: 1.486 GB
-# read + 183.7 MB written); scaled to the average launch for roofline.traffic.
-EXTEND_DRAM_BYTES_PER_RAY = 199.0
+# 8,388,608-ray launch on the terrain (profiles/trace_single_terrain_ncu.md: 1.501 GB
+# read + 189.3 MB written); scaled to the average launch for roofline.traffic.
+EXTEND_DRAM_BYTES_PER_RAY = 201.5
 
 
 def parse():
