@@ -1320,7 +1320,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
                 ++launches;
             }
             if (prof) cudaEventRecord(ev[3], st);
-            launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, gShade, st);
+            launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, ctx->numSMs, st);
             if (prof) cudaEventRecord(ev[4], st);
             launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, ctx->numSMs, st);
             if (prof) cudaEventRecord(ev[5], st);

@@ -149,7 +149,7 @@ void enqueueBlock(BatchState* b, const BatchView& v, unsigned int cap, int iters
         launchPlan(b->ctrl, cap, st);
         launchGenerateBatch(v, X, b->ctrl, numSMs * 8, st);
         launchExtendBatch(v, X, b->hits, b->ctrl, numSMs, st);
-        launchShadeBatch(v, X, b->hits, Y, b->shadow, b->ctrl, numSMs * 8, st);
+        launchShadeBatch(v, X, b->hits, Y, b->shadow, b->ctrl, numSMs, st);
         launchShadowBatch(v, b->shadow, Y, b->ctrl, numSMs, st);
     }
 }

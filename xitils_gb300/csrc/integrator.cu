@@ -79,15 +79,15 @@ void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctr
 }
 
 void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
-                 Ctrl* ctrl, int grid, cudaStream_t s) {
+                 Ctrl* ctrl, int numSMs, cudaStream_t s) {
     const OneJob job{sc, rp};
     switch (sc.nested & 3) {
-    case 1: launchShadeMask1(job, in, h, out, sq, ctrl, grid, s); break;
-    case 2: launchShadeMask2(job, in, h, out, sq, ctrl, grid, s); break;
-    case 3: launchShadeMask3(job, in, h, out, sq, ctrl, grid, s); break;
+    case 1: launchShadeMask1(job, in, h, out, sq, ctrl, numSMs, s); break;
+    case 2: launchShadeMask2(job, in, h, out, sq, ctrl, numSMs, s); break;
+    case 3: launchShadeMask3(job, in, h, out, sq, ctrl, numSMs, s); break;
     default:
-        if (rp.guided || rp.train || rp.aov) k_shade<OneJob, 0, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
-        else k_shade<OneJob, 0, false><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+        if (rp.guided || rp.train || rp.aov) launchShadeVariant<OneJob, 0, true>(job, in, h, out, sq, ctrl, numSMs, s);
+        else launchShadeVariant<OneJob, 0, false>(job, in, h, out, sq, ctrl, numSMs, s);
         break;
     }
 }
@@ -96,11 +96,11 @@ void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, 
     k_generate<ManyJobs><<<grid, kShadeBlock, 0, s>>>(ManyJobs{b.scenes, b.params, b.start, b.nJobs}, q, ctrl);
 }
 
-void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
-                      cudaStream_t s) {
+void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
+                      int numSMs, cudaStream_t s) {
     const ManyJobs jobs{b.scenes, b.params, b.start, b.nJobs};
-    if (b.nested) launchShadeMask3Batch(jobs, in, h, out, sq, ctrl, grid, s);
-    else k_shade<ManyJobs, 0, false><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+    if (b.nested) launchShadeMask3Batch(jobs, in, h, out, sq, ctrl, numSMs, s);
+    else launchShadeVariant<ManyJobs, 0, false>(jobs, in, h, out, sq, ctrl, numSMs, s);
 }
 
 }  // namespace xgb

@@ -150,7 +150,7 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
             launchPlan(ctrl, cap, st);
             launchGenerate(sd, rp, X, ctrl, gShade, st);
             launchExtend(sd, X, hits, ctrl, numSMs, false, st);
-            launchShade(sd, rp, X, hits, Y, sq, ctrl, gShade, st);
+            launchShade(sd, rp, X, hits, Y, sq, ctrl, numSMs, st);
             launchShadow(sd, rp, sq, Y, ctrl, numSMs, st);
             parity ^= 1;
         }

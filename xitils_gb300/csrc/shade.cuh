@@ -444,18 +444,47 @@ __global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, P
     }
 }
 
+// Grid of a shade launch: kShadeWaves full waves of the variant's resident
+// blocks (SMs x blocks per SM at its register bound). Whole waves leave no
+// partial last wave idling SMs (eight blocks per SM at three resident ran as
+// 2.67 waves); many small blocks let SMs whose blocks finish early take more,
+// which the uneven per-path cost of nested materials needs. Measured on GB300,
+// shading time per render against the earlier eight blocks per SM: one wave --
+// terrain 12.1 instead of 12.6 ms, normal mapping 5.96 instead of 4.4; four
+// waves -- 12.7 / 4.4; eight waves -- terrain 12.6, shell mapping 7.6 instead
+// of 8.6, normal mapping 3.6.
+constexpr int kShadeWaves = 8;
+template <class J, int NESTED, bool EXTRAS>
+inline int shadeGrid(int numSMs) {
+    static int perSM = 0;
+    if (perSM == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<J, NESTED, EXTRAS>, kShadeBlock, 0) != cudaSuccess ||
+            b < 1)
+            b = 1;
+        perSM = b;
+    }
+    return numSMs * perSM * kShadeWaves;
+}
+
+template <class J, int NESTED, bool EXTRAS>
+inline void launchShadeVariant(const J& jobs, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
+                               int numSMs, cudaStream_t s) {
+    k_shade<J, NESTED, EXTRAS><<<shadeGrid<J, NESTED, EXTRAS>(numSMs), kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+}
+
 // Launches of the shade variants for scenes with materials that evaluate another
 // (the mask: 1 microfacet normal mapping, 2 MultiLobeSVBRDF, 3 both), compiled in
 // their own translation units so that the build compiles them in parallel:
 // shade_layered.cu (masks 1 and 2), shade_nested.cu (mask 3, one scene),
 // shade_batch_nested.cu (mask 3, a batch).
-void launchShadeMask1(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask1(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s);
-void launchShadeMask2(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask2(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s);
-void launchShadeMask3(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask3(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s);
 void launchShadeMask3Batch(const ManyJobs& jobs, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
-                           int grid, cudaStream_t s);
+                           int numSMs, cudaStream_t s);
 
 }  // namespace xgb

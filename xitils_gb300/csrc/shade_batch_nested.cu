@@ -6,8 +6,8 @@
 namespace xgb {
 
 void launchShadeMask3Batch(const ManyJobs& jobs, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
-                           int grid, cudaStream_t s) {
-    k_shade<ManyJobs, 3, false><<<grid, kShadeBlock, 0, s>>>(jobs, in, h, out, sq, ctrl);
+                           int numSMs, cudaStream_t s) {
+    launchShadeVariant<ManyJobs, 3, false>(jobs, in, h, out, sq, ctrl, numSMs, s);
 }
 
 }  // namespace xgb

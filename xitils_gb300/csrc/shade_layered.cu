@@ -4,14 +4,14 @@
 
 namespace xgb {
 
-void launchShadeMask1(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask1(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s) {
-    k_shade<OneJob, 1, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    launchShadeVariant<OneJob, 1, true>(job, in, h, out, sq, ctrl, numSMs, s);
 }
 
-void launchShadeMask2(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask2(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s) {
-    k_shade<OneJob, 2, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    launchShadeVariant<OneJob, 2, true>(job, in, h, out, sq, ctrl, numSMs, s);
 }
 
 }  // namespace xgb

@@ -4,9 +4,9 @@
 
 namespace xgb {
 
-void launchShadeMask3(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
+void launchShadeMask3(const OneJob& job, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int numSMs,
                       cudaStream_t s) {
-    k_shade<OneJob, 3, true><<<grid, kShadeBlock, 0, s>>>(job, in, h, out, sq, ctrl);
+    launchShadeVariant<OneJob, 3, true>(job, in, h, out, sq, ctrl, numSMs, s);
 }
 
 }  // namespace xgb

@@ -143,18 +143,18 @@ struct BatchView {
     int nested;  // some scene has a material that evaluates another (the shade kernel with that code)
 };
 void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
-void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl, int grid,
-                      cudaStream_t s);
+void launchShadeBatch(const BatchView& b, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq, Ctrl* ctrl,
+                      int numSMs, cudaStream_t s);
 void launchExtendBatch(const BatchView& b, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, cudaStream_t s);
 void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs, cudaStream_t s);
 
 void launchPlan(Ctrl* ctrl, unsigned int capacity, cudaStream_t s);
 void launchGenerate(const SceneDev& sc, const RenderParams& rp, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
-// Extension / shadow rays of the wavefront; persistent grids sized from the
-// launched kernel's occupancy on numSMs SMs.
+// Extension / shadow rays and shading of the wavefront; grids sized from the
+// launched kernel's occupancy on numSMs SMs (one full wave).
 void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, bool count, cudaStream_t s);
 void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQueue h, PathQueue out, ShadowQueue sq,
-                 Ctrl* ctrl, int grid, cudaStream_t s);
+                 Ctrl* ctrl, int numSMs, cudaStream_t s);
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s);
 // Ray queries on a built scene: rays o (xyz, w = tMax) and d; closest hits as 2 float4
