@@ -56,6 +56,16 @@ NODE_BYTES, TRI_BYTES = 64, 48
 EXTEND_DRAM_BYTES_PER_RAY = 201.5
 
 
+def wavefront_bytes(paths: int, ext: int, shadow: int) -> int:
+    """Algorithmic queue bytes of the whole wavefront, from the record sizes of the
+    path, hit and shadow queues: generate writes a 56 B path per camera path; extend
+    reads the 32 B ray and writes a 20 B hit; shade reads the 56 B path and the hit,
+    writes a 56 B path per continuing path (extension rays - paths) and a 56 B
+    shadow record per shadow ray, of which the shadow kernel reads 48 B. Film
+    atomics, texture and BVH reads are data-dependent and not counted."""
+    return 56 * paths + (52 + 76) * ext + 56 * (ext - paths) + (56 + 48) * shadow
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -526,6 +536,15 @@ def run_xgb(args):
         "nodes_per_ray": agg["node_visits"] / max(agg["extension_rays"], 1),
         "tris_per_ray": agg["tri_tests"] / max(agg["extension_rays"], 1),
     }
+    total_ms = sum(stage_ms)
+    wf_bytes = wavefront_bytes(agg["paths"], agg["extension_rays"], agg["shadow_rays"])
+    wf_achieved = wf_bytes / (total_ms / 1e3) / 1e9 if total_ms > 0 else None
+    wavefront = {
+        "what": "queue records of all five stages (generate, extend, shade, shadow) over the summed stage time",
+        "bound": "hbm", "unit": "GB/s", "achieved": wf_achieved, "peak": hbm if hbm else 6800.0,
+        "frac": (wf_achieved / (hbm or 6800.0)) if wf_achieved else None,
+        "bytes_per_path": wf_bytes / max(agg["paths"], 1),
+    }
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -559,6 +578,7 @@ def run_xgb(args):
         "gpu_launches": agg["kernel_launches"] // len(stats) * args.steps,
         "mrays_per_s": total_rays / len(stats) * args.steps * world / (ms_max / 1e3) / 1e6,
         "roofline": roofline,
+        "wavefront_roofline": wavefront,
         "cpu_baseline": cpu,
         "clocks": clk,
         "stage_ms": {"plan": stage_ms[0], "generate": stage_ms[1], "extend": stage_ms[2], "shade": stage_ms[3],
