@@ -86,7 +86,7 @@ def parse():
     p.add_argument("--no-guided", action="store_true")
     p.add_argument("--guided-res", type=int, default=512)
     p.add_argument("--guided-seconds", type=float, default=8.0)
-    p.add_argument("--guided-ref-spp", type=int, default=8192)
+    p.add_argument("--guided-ref-spp", type=int, default=16384)
     p.add_argument("--guided-pass-spp", type=int, default=16)
     p.add_argument("--guided-train-pass-spp", type=int, default=4)
     p.add_argument("--guided-max-steps", type=int, default=512)
