@@ -60,10 +60,11 @@ __global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, c
         d = xformVector(sc.c2w, d);
         // Standard: the first loop vertex has pathLength 2; Naive counts from 1.
         int len = rp.integrator == 0 ? 2 : 1;
-        q.o[s] = make_float4(o.x, o.y, o.z, 0.0f);
-        q.d[s] = make_float4(d.x, d.y, d.z, __int_as_float(len | (FLAG_PRIMARY << 16)));
-        q.thr[s] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(jobs.encode(job, (int)pix)));
-        q.rng[s] = make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32));
+        // streaming stores: the queue is read once, by the next traversal
+        __stcs(&q.o[s], make_float4(o.x, o.y, o.z, 0.0f));
+        __stcs(&q.d[s], make_float4(d.x, d.y, d.z, __int_as_float(len | (FLAG_PRIMARY << 16))));
+        __stcs(&q.thr[s], make_float4(1.0f, 1.0f, 1.0f, __int_as_float(jobs.encode(job, (int)pix))));
+        __stcs(&q.rng[s], make_uint2((unsigned int)rng.state, (unsigned int)(rng.state >> 32)));
         if (rp.train) {
             q.grec[s] = -1;
             q.pid[s] = (unsigned int)g;

@@ -198,10 +198,14 @@ __global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, P
         r.stochastic = false;
         r.grec = -1;
         if (i < n) {
-            float4 o4 = in.o[i], d4 = in.d[i], t4 = in.thr[i];
-            uint2 rs = in.rng[i];
-            float4 h = hq.h[i];
-            const int instId = hq.inst[i];
+            // Queue records are read once and written once per iteration and far
+            // exceed L2 at 2^23 paths in flight: streaming (evict-first) loads and
+            // stores keep L2 for BVH nodes, triangles and textures (terrain shading
+            // 12.7 -> 11.6 ms per render, 1495 -> 1533 Mpaths/s on GB300).
+            float4 o4 = __ldcs(&in.o[i]), d4 = __ldcs(&in.d[i]), t4 = __ldcs(&in.thr[i]);
+            uint2 rs = __ldcs(&in.rng[i]);
+            float4 h = __ldcs(&hq.h[i]);
+            const int instId = __ldcs(&hq.inst[i]);
             const int prim = __float_as_int(h.w);
             const int meta = __float_as_int(d4.w);
             int len = meta & 0xFFFF;
@@ -417,10 +421,10 @@ __global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, P
         unsigned int slot = oc + __popc(mc & ((1u << lane) - 1u));
         const bool train = EXTRAS && jobs.params(0).train;  // guide training runs with one job only
         if (cont) {
-            out.o[slot] = r.o;
-            out.d[slot] = r.d;
-            out.thr[slot] = r.thr;
-            out.rng[slot] = r.rng;
+            __stcs(&out.o[slot], r.o);
+            __stcs(&out.d[slot], r.d);
+            __stcs(&out.thr[slot], r.thr);
+            __stcs(&out.rng[slot], r.rng);
             if (train) {
                 out.grec[slot] = r.grec;
                 out.pid[slot] = in.pid[i];
@@ -432,11 +436,11 @@ __global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, P
         os = __shfl_sync(kFull, os, 0);
         if (shadow) {
             unsigned int ss = os + __popc(ms & ((1u << lane) - 1u));
-            sq.o[ss] = r.so;
-            sq.d[ss] = r.sd;
+            __stcs(&sq.o[ss], r.so);
+            __stcs(&sq.d[ss], r.sd);
             r.sc.w = __int_as_float((r.stochastic && cont) ? (int)slot : -1);
-            sq.c[ss] = r.sc;
-            sq.rng[ss] = r.srng;
+            __stcs(&sq.c[ss], r.sc);
+            __stcs(&sq.rng[ss], r.srng);
             if (train) sq.pid[ss] = in.pid[i];
         }
         unsigned int md = __ballot_sync(kFull, done);

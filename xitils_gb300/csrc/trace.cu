@@ -187,8 +187,9 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
             ray = base + __popc(act & ltMask);
             if (ray >= n) break;
             float4 o4, d4;
-            if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
-            else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
+            // queue records: streaming loads / stores, as in k_shade
+            if (ANY) { o4 = __ldcs(&s.o[ray]); d4 = __ldcs(&s.d[ray]); tMax = o4.w; }
+            else { o4 = __ldcs(&q.o[ray]); d4 = __ldcs(&q.d[ray]); tMax = __int_as_float(0x7f800000); }
             wo = V3(o4.x, o4.y, o4.z);
             wd = V3(d4.x, d4.y, d4.z);
             br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
@@ -217,8 +218,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
                         if (rp.train) creditPath(rp, s.pid[ray], cc);
                     }
                 } else {
-                    h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
-                    h.inst[ray] = hit.inst;
+                    __stcs(&h.h[ray], make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim)));
+                    __stcs(&h.inst[ray], hit.inst);
                 }
                 fetch = true;
             } else {
@@ -365,8 +366,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             ray = base + __popc(act & ltMask);
             if (ray >= n) break;
             float4 o4, d4;
-            if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
-            else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
+            if (ANY) { o4 = __ldcs(&s.o[ray]); d4 = __ldcs(&s.d[ray]); tMax = o4.w; }
+            else { o4 = __ldcs(&q.o[ray]); d4 = __ldcs(&q.d[ray]); tMax = __int_as_float(0x7f800000); }
             wo = V3(o4.x, o4.y, o4.z);
             wd = V3(d4.x, d4.y, d4.z);
             br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
@@ -398,8 +399,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
                         if (rp.train) creditPath(rp, s.pid[ray], cc);
                     }
                 } else {
-                    h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
-                    h.inst[ray] = hit.inst;
+                    __stcs(&h.h[ray], make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim)));
+                    __stcs(&h.inst[ray], hit.inst);
                 }
                 fetch = true;
                 continue;
@@ -529,8 +530,8 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             ray = base + __popc(act & ltMask);
             if (ray >= n) break;
             float4 o4, d4;
-            if (ANY) { o4 = s.o[ray]; d4 = s.d[ray]; tMax = o4.w; }
-            else { o4 = q.o[ray]; d4 = q.d[ray]; tMax = __int_as_float(0x7f800000); }
+            if (ANY) { o4 = __ldcs(&s.o[ray]); d4 = __ldcs(&s.d[ray]); tMax = o4.w; }
+            else { o4 = __ldcs(&q.o[ray]); d4 = __ldcs(&q.d[ray]); tMax = __int_as_float(0x7f800000); }
             V3 o(o4.x, o4.y, o4.z), d(d4.x, d4.y, d4.z);
             if (!identity) {
                 o = xformPointRn(in.matInv, o);
@@ -603,8 +604,8 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
                     if (rp.train) creditPath(rp, s.pid[ray], cc);
                 }
             } else {
-                h.h[ray] = make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim));
-                h.inst[ray] = hit.prim >= 0 ? 0 : -1;
+                __stcs(&h.h[ray], make_float4(hit.prim >= 0 ? hit.t : tMax, hit.b0, hit.b1, __int_as_float(hit.prim)));
+                __stcs(&h.inst[ray], hit.prim >= 0 ? 0 : -1);
             }
         }
     }
