@@ -460,14 +460,14 @@ __global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, P
 constexpr int kShadeWaves = 8;
 template <class J, int NESTED, bool EXTRAS>
 inline int shadeGrid(int numSMs) {
-    static int perSM = 0;
-    if (perSM == 0) {
+    // looked up once per variant (a thread-safe static initialisation)
+    static const int perSM = [] {
         int b = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_shade<J, NESTED, EXTRAS>, kShadeBlock, 0) != cudaSuccess ||
             b < 1)
             b = 1;
-        perSM = b;
-    }
+        return b;
+    }();
     return numSMs * perSM * kShadeWaves;
 }
 
