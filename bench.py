@@ -94,6 +94,7 @@ def parse():
 
 
 SINGLE_KERNEL = "k_trace_single (closest-hit traversal of a one-instance scene, binary BVH, persistent)"
+FLAT_KERNEL = "k_trace_flat2 (closest-hit traversal of a scene of <= 16 instances, binary BVHs, persistent)"
 
 
 def make_workload(args):
@@ -121,14 +122,14 @@ def make_workload(args):
                  f"Cornell-style room, {res}x{res} film, {spp} spp, reference defaults "
                  f"(no depth limit, RR after 5 at 0.9)")
         meta = {"data": "synthetic (seeded cloth patch, procedural plain-weave displacement map)",
-                "kernel": "k_extend (two-level closest-hit traversal with the shell-mapping discard, persistent)",
+                "kernel": "k_trace_flat2 (closest-hit traversal of <= 16 instances with the shell-mapping discard, persistent)",
                 "l2": big}
     else:
         res = args.res or 512
         spp = args.spp or 16
         desc = scenes.cornell(res, res, spp)
         label = f"cornell 36 tris, {res}x{res} film, {spp} spp, max depth 8, RR after depth 3"
-        meta = {"data": "synthetic (the Cornell box of the workload description)", "kernel": SINGLE_KERNEL,
+        meta = {"data": "synthetic (the Cornell box of the workload description)", "kernel": FLAT_KERNEL,
                 "l2": "the scene fits in L2 (36 triangles); path queues of 2^23 paths stream through HBM"}
     return desc, label, meta
 
@@ -527,8 +528,11 @@ def run_xgb(args):
         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "fallback 6.8 TB/s",
         "unit": "GB/s",
         "frac": (achieved / (hbm or 6800.0)) if achieved else None,
-        "traffic": EXTEND_DRAM_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
-        "traffic_source": "ncu dram__bytes_read+write per ray (profiles/trace_single_terrain_ncu.md) x rays per launch",
+        # the DRAM bytes per ray come from the terrain's ncu capture; other workloads have none
+        "traffic": (EXTEND_DRAM_BYTES_PER_RAY * agg["extension_rays"] / ext_launches
+                    if args.workload == "terrain" else None),
+        "traffic_source": ("ncu dram__bytes_read+write per ray (profiles/trace_single_terrain_ncu.md) x rays per launch"
+                           if args.workload == "terrain" else "no ncu capture of this workload"),
         "algorithmic_bytes_per_launch": EXTEND_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
         "avg_launch_ms": ext_ms / ext_launches,
         "bvh_l2_gbs": ((NODE_BYTES * agg["node_visits"] + TRI_BYTES * agg["tri_tests"]) / (ext_ms / 1e3) / 1e9
