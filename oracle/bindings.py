@@ -125,6 +125,26 @@ class CpuChecker:
         assert r >= 0, "add_material failed"
         return r
 
+    def bsdf_sample(self, material, wo, n, seed=0):
+        """n draws of the material's evalAndSample at the flat shading point of
+        scene_api.h: (wi [n, 3], weight [n, 3], pdf [n]); draw k on stream (k, 0, seed)."""
+        wo = np.ascontiguousarray(wo, dtype=np.float32).reshape(3)
+        out = np.zeros((n, 7), np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        r = self._call("bsdf_sample_pcg", C.c_int(material), fp(wo), C.c_int(n), C.c_uint32(seed), fp(out))
+        assert r == 0, r
+        return out[:, :3], out[:, 3:6], out[:, 6]
+
+    def bsdf_eval(self, material, wo, wi, seed=0):
+        """getPDF and bsdfCos of the material for each direction wi [n, 3]: (pdf [n], f [n, 3])."""
+        wo = np.ascontiguousarray(wo, dtype=np.float32).reshape(3)
+        wi = np.ascontiguousarray(wi, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros((len(wi), 4), np.float32)
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        r = self._call("bsdf_eval_pcg", C.c_int(material), fp(wo), C.c_int(len(wi)), fp(wi), C.c_uint32(seed), fp(out))
+        assert r == 0, r
+        return out[:, 0], out[:, 1:]
+
     def add_object(self, mesh, material, mat, matInv):
         m = np.ascontiguousarray(mat, dtype=np.float32)
         mi = np.ascontiguousarray(matInv, dtype=np.float32)

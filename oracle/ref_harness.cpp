@@ -291,6 +291,59 @@ int xref_vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs) 
     return 0;
 }
 
+// Flat shading point of the per-material queries (scene_api.h), as a
+// SurfaceIntersection (Interaction.h:16-32).
+static SurfaceIntersection flatIsect(const float* wo) {
+    SurfaceIntersection is;
+    is.p = Vector3f(0, 0, 0);
+    is.wo = Vector3f(wo[0], wo[1], wo[2]);
+    is.n = is.shading.n = Vector3f(0, 0, 1);
+    is.tangent = is.shading.tangent = Vector3f(1, 0, 0);
+    is.bitangent = is.shading.bitangent = Vector3f(0, 1, 0);
+    is.texCoord = Vector2f(0.5f, 0.5f);
+    return is;
+}
+
+int xref_bsdf_sample_pcg(void* p, int material, const float* wo, int n, uint32_t seed, float* out) {
+    RefScene* s = (RefScene*)p;
+    if (!s || !wo || !out || n < 0 || material < 0 || material >= (int)s->materials.size()) return -1;
+    const SurfaceIntersection is = flatIsect(wo);
+    PcgSampler sampler;
+    try {
+        for (int k = 0; k < n; ++k) {
+            sampler.seedPath((uint32_t)k, 0, seed);
+            Vector3f wi(0, 0, 0);
+            float pdf = 0.0f;
+            Vector3f f = s->materials[material]->evalAndSample(is, sampler, &wi, &pdf);
+            float* o = out + 7 * (size_t)k;
+            o[0] = wi.x; o[1] = wi.y; o[2] = wi.z; o[3] = f.x; o[4] = f.y; o[5] = f.z; o[6] = pdf;
+        }
+    } catch (...) {
+        return -2;
+    }
+    return 0;
+}
+
+int xref_bsdf_eval_pcg(void* p, int material, const float* wo, int n, const float* wi, uint32_t seed, float* out) {
+    RefScene* s = (RefScene*)p;
+    if (!s || !wo || !wi || !out || n < 0 || material < 0 || material >= (int)s->materials.size()) return -1;
+    const SurfaceIntersection is = flatIsect(wo);
+    PcgSampler sampler;
+    try {
+        for (int k = 0; k < n; ++k) {
+            sampler.seedPath((uint32_t)k, 1, seed);
+            const Vector3f w(wi[3 * k], wi[3 * k + 1], wi[3 * k + 2]);
+            float pdf = s->materials[material]->getPDF(is, w);
+            Vector3f f = s->materials[material]->bsdfCos(is, sampler, w);
+            float* o = out + 4 * (size_t)k;
+            o[0] = pdf; o[1] = f.x; o[2] = f.y; o[3] = f.z;
+        }
+    } catch (...) {  // specular materials and Emission throw NOT_IMPLEMENTED (Utils.h:27)
+        return -2;
+    }
+    return 0;
+}
+
 int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
     RefScene* s = (RefScene*)p;
     std::shared_ptr<Material> m;

@@ -14,6 +14,16 @@
  *   matrices: float[16] row-major m[r][c] (Xitils Matrix4x4 layout);
  *   textures: packed float RGB [h][w][3], row y = 0 first (Texture.h:41-80);
  *   films: float RGB sums [H][W][3], pixel (x, y) at (x + y * W) (RenderTarget.h:25-27).
+ *
+ * Per-material BSDF queries (the materials' unit tests): a flat shading point at the
+ * origin with n = shading.n = +z, tangent +x, bitangent +y, texcoord (0.5, 0.5) and the
+ * given wo (unit, any side).
+ *   bsdf_sample_pcg: n draws of Material::evalAndSample, draw k on the PCG stream
+ *     (k, 0, seed): out[k] = wi.xyz, returned weight rgb, pdf (7 floats; a zero
+ *     weight leaves wi and pdf undefined, as in Material.h:21-25).
+ *   bsdf_eval_pcg: for each wi[k], getPDF and bsdfCos (a stochastic bsdfCos draws on
+ *     the stream (k, 1, seed)): out[k] = pdf, rgb (4 floats). Specular materials
+ *     have neither; the call returns -2 for them.
  */
 #ifndef XGB_ORACLE_SCENE_API_H
 #define XGB_ORACLE_SCENE_API_H
@@ -51,6 +61,10 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
                      uint32_t seed, float* low_r, float* lobes);                                     \
     int P##vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs);                  \
     int P##add_material(void* s, int type, const float* f, int base, int tex, int normalmap);      \
+    int P##bsdf_sample_pcg(void* s, int material, const float* wo, int n, uint32_t seed,           \
+                           float* out);                                                            \
+    int P##bsdf_eval_pcg(void* s, int material, const float* wo, int n, const float* wi,           \
+                         uint32_t seed, float* out);                                               \
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \
     int P##set_sky(void* s, int type, const float* rgb, int tex);                                  \

@@ -1503,6 +1503,58 @@ int xcpu_vmf4_sample_pcg(const float* lobes, int n, uint32_t seed, float* dirs) 
     return 0;
 }
 
+// Flat shading point of the per-material queries (scene_api.h).
+static Isect flatIsect(const float* wo) {
+    Isect is;
+    is.p = V3(0, 0, 0);
+    is.wo = V3(wo[0], wo[1], wo[2]);
+    is.n = is.sn = V3(0, 0, 1);
+    is.tangent = is.stangent = V3(1, 0, 0);
+    is.bitangent = is.sbitangent = V3(0, 1, 0);
+    is.uv = V2(0.5f, 0.5f);
+    return is;
+}
+
+static bool specularKind(int type) {
+    return type == ORC_MAT_SPECULAR_REFLECTION || type == ORC_MAT_SPECULAR_REFRACTION ||
+           type == ORC_MAT_SPECULAR_FRESNEL || type == ORC_MAT_EMISSION;
+}
+
+int xcpu_bsdf_sample_pcg(void* s, int material, const float* wo, int n, uint32_t seed, float* out) {
+    const Scene* sc = (const Scene*)s;
+    if (!sc || !wo || !out || n < 0 || material < 0 || material >= (int)sc->materials.size()) return -1;
+    const Isect is = flatIsect(wo);
+    const Shading sh{sc};
+    for (int k = 0; k < n; ++k) {
+        Rng rng;
+        rng.seed((uint32_t)k, 0, seed);
+        V3 wi;
+        float pdf = 0.0f;
+        V3 f = sh.evalAndSample(material, is, rng, &wi, &pdf);
+        float* o = out + 7 * (size_t)k;
+        o[0] = wi.x; o[1] = wi.y; o[2] = wi.z; o[3] = f.x; o[4] = f.y; o[5] = f.z; o[6] = pdf;
+    }
+    return 0;
+}
+
+int xcpu_bsdf_eval_pcg(void* s, int material, const float* wo, int n, const float* wi, uint32_t seed, float* out) {
+    const Scene* sc = (const Scene*)s;
+    if (!sc || !wo || !wi || !out || n < 0 || material < 0 || material >= (int)sc->materials.size()) return -1;
+    if (specularKind(sc->materials[material].type)) return -2;
+    const Isect is = flatIsect(wo);
+    const Shading sh{sc};
+    for (int k = 0; k < n; ++k) {
+        Rng rng;
+        rng.seed((uint32_t)k, 1, seed);
+        const V3 w(wi[3 * k], wi[3 * k + 1], wi[3 * k + 2]);
+        float pdf = sh.getPDF(material, is, w);
+        V3 f = sh.bsdfCos(material, is, rng, w);
+        float* o = out + 4 * (size_t)k;
+        o[0] = pdf; o[1] = f.x; o[2] = f.y; o[3] = f.z;
+    }
+    return 0;
+}
+
 int xcpu_add_material(void* s, int type, const float* f, int base, int tex, int normalmap) {
     Scene* sc = (Scene*)s;
     Material m;
