@@ -146,3 +146,24 @@ def test_sampling_follows_the_reported_density(name, theta):
     dof = int(keep.sum()) - 1
     p = chi2.sf(stat, dof)
     assert p > 1e-4, (name, theta, stat, dof, p)
+
+
+def test_metal_leaks_below_the_horizon_unless_fixed():
+    """Metal's VNDF sampling reflects wo about a visible normal, which can send wi below
+    the shading normal; the reference keeps those samples with a non-zero weight
+    (G1 squares the cosine, Material.h:309-316, 323-345). The opt-in horizon fix
+    (XGB_FIX_METAL_HORIZON, material parameter 4 of the checkers) drops them."""
+    c = CpuChecker("port")
+    leak = c.add_material(METAL, [0.7, 0.9, 0.9, 0.9, 0])
+    fixed = c.add_material(METAL, [0.7, 0.9, 0.9, 0.9, 1])
+    wo = _wo(80.0)
+    wi, f, pdf = c.bsdf_sample(leak, wo, 20_000, seed=5)
+    below = (wi[:, 2] < 0) & (np.abs(f).sum(1) > 0)
+    assert below.mean() > 0.01
+    wi, f, pdf = c.bsdf_sample(fixed, wo, 20_000, seed=5)
+    assert not ((wi[:, 2] < 0) & (np.abs(f).sum(1) > 0)).any()
+    if REF is not None:
+        ref, _ = REF
+        m = ref.add_material(METAL, [0.7, 0.9, 0.9, 0.9, 0])
+        wr, fr, pr = ref.bsdf_sample(m, wo, 20_000, seed=5)
+        assert ((wr[:, 2] < 0) & (np.abs(fr).sum(1) > 0)).mean() == below.mean()
