@@ -145,6 +145,14 @@ class CpuChecker:
         assert r == 0, r
         return out[:, 0], out[:, 1:]
 
+    def light_sample(self, n, seed=0):
+        """n draws of Scene::sampleSurface on a built scene: (p [n, 3], n [n, 3], pdf [n]);
+        draw k on stream (k, 2, seed)."""
+        out = np.zeros((n, 7), np.float32)
+        r = self._call("light_sample_pcg", C.c_int(n), C.c_uint32(seed), out.ctypes.data_as(C.POINTER(C.c_float)))
+        assert r == 0, r
+        return out[:, :3], out[:, 3:6], out[:, 6]
+
     def add_object(self, mesh, material, mat, matInv):
         m = np.ascontiguousarray(mat, dtype=np.float32)
         mi = np.ascontiguousarray(matInv, dtype=np.float32)

@@ -344,6 +344,22 @@ int xref_bsdf_eval_pcg(void* p, int material, const float* wo, int n, const floa
     return 0;
 }
 
+int xref_light_sample_pcg(void* p, int n, uint32_t seed, float* out) {
+    RefScene* s = (RefScene*)p;
+    if (!s || !out || n < 0) return -1;
+    if (!s->built) return -3;
+    if (!s->scene.canSampleLight()) return -2;
+    PcgSampler sampler;
+    for (int k = 0; k < n; ++k) {
+        sampler.seedPath((uint32_t)k, 2, seed);
+        float pdf = 0.0f;
+        auto ls = s->scene.sampleSurface(sampler, &pdf);
+        float* o = out + 7 * (size_t)k;
+        o[0] = ls.p.x; o[1] = ls.p.y; o[2] = ls.p.z; o[3] = ls.n.x; o[4] = ls.n.y; o[5] = ls.n.z; o[6] = pdf;
+    }
+    return 0;
+}
+
 int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
     RefScene* s = (RefScene*)p;
     std::shared_ptr<Material> m;

@@ -24,6 +24,10 @@
  *   bsdf_eval_pcg: for each wi[k], getPDF and bsdfCos (a stochastic bsdfCos draws on
  *     the stream (k, 1, seed)): out[k] = pdf, rgb (4 floats). Specular materials
  *     have neither; the call returns -2 for them.
+ *
+ * light_sample_pcg (built scenes only, -3 otherwise): n draws of Scene::sampleSurface
+ * (Scene.h:40-47), draw k on the PCG stream (k, 2, seed): out[k] = p.xyz, geometric
+ * normal n.xyz, pdf (area measure) (7 floats).
  */
 #ifndef XGB_ORACLE_SCENE_API_H
 #define XGB_ORACLE_SCENE_API_H
@@ -65,6 +69,7 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
                            float* out);                                                            \
     int P##bsdf_eval_pcg(void* s, int material, const float* wo, int n, const float* wi,           \
                          uint32_t seed, float* out);                                               \
+    int P##light_sample_pcg(void* s, int n, uint32_t seed, float* out);                            \
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \
     int P##set_sky(void* s, int type, const float* rgb, int tex);                                  \

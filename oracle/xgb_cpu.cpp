@@ -1555,6 +1555,22 @@ int xcpu_bsdf_eval_pcg(void* s, int material, const float* wo, int n, const floa
     return 0;
 }
 
+int xcpu_light_sample_pcg(void* s, int n, uint32_t seed, float* out) {
+    const Scene* sc = (const Scene*)s;
+    if (!sc || !out || n < 0) return -1;
+    if (!sc->built) return -3;
+    if (sc->lights.empty()) return -2;
+    for (int k = 0; k < n; ++k) {
+        Rng rng;
+        rng.seed((uint32_t)k, 2, seed);
+        float pdf = 0.0f;
+        LightSample ls = sampleLight(*sc, rng, &pdf);
+        float* o = out + 7 * (size_t)k;
+        o[0] = ls.p.x; o[1] = ls.p.y; o[2] = ls.p.z; o[3] = ls.n.x; o[4] = ls.n.y; o[5] = ls.n.z; o[6] = pdf;
+    }
+    return 0;
+}
+
 int xcpu_add_material(void* s, int type, const float* f, int base, int tex, int normalmap) {
     Scene* sc = (Scene*)s;
     Material m;
