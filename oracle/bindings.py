@@ -153,6 +153,24 @@ class CpuChecker:
         assert r == 0, r
         return out[:, :3], out[:, 3:6], out[:, 6]
 
+    def intersect(self, rays):
+        """Scene::intersect of float32 [n, 7] rays (o, d, tMax) -> (t [n], object [n], p [n, 3],
+        shading normal [n, 3]); object -1 on a miss."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        out = np.zeros((rays.shape[0], 8), np.float32)
+        r = self._call("intersect", C.c_int(rays.shape[0]), rays.ctypes.data_as(C.POINTER(C.c_float)),
+                       out.ctypes.data_as(C.POINTER(C.c_float)))
+        assert r == 0, r
+        return out[:, 0], out[:, 1].astype(np.int32), out[:, 2:5], out[:, 5:8]
+
+    def intersect_any(self, rays):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        out = np.zeros(rays.shape[0], np.int32)
+        r = self._call("intersect_any", C.c_int(rays.shape[0]), rays.ctypes.data_as(C.POINTER(C.c_float)),
+                       out.ctypes.data_as(C.POINTER(C.c_int32)))
+        assert r == 0, r
+        return out
+
     def add_object(self, mesh, material, mat, matInv):
         m = np.ascontiguousarray(mat, dtype=np.float32)
         mi = np.ascontiguousarray(matInv, dtype=np.float32)

@@ -126,6 +126,7 @@ struct RefScene {
     std::vector<std::shared_ptr<SVNDF>> svndfs;
     std::vector<std::shared_ptr<Texture>> svndfLow;
     std::vector<float> svndfScale;
+    std::vector<const Object*> objects;  // in add_object order, for the queries' object index
     bool built = false;
     int serial = 0;
 };
@@ -360,6 +361,40 @@ int xref_light_sample_pcg(void* p, int n, uint32_t seed, float* out) {
     return 0;
 }
 
+int xref_intersect(void* p, int n, const float* rays, float* out) {
+    RefScene* s = (RefScene*)p;
+    if (!s || !rays || !out || n < 0) return -1;
+    if (!s->built) return -3;
+    for (int i = 0; i < n; ++i) {
+        Ray r(Vector3f(rays[7 * i], rays[7 * i + 1], rays[7 * i + 2]),
+              Vector3f(rays[7 * i + 3], rays[7 * i + 4], rays[7 * i + 5]), rays[7 * i + 6]);
+        SurfaceIntersection is;
+        float* o = out + 8 * (size_t)i;
+        const bool hit = s->scene.intersect(r, &is);
+        int obj = -1;
+        if (hit)
+            for (size_t k = 0; k < s->objects.size(); ++k)
+                if (s->objects[k] == is.object) obj = (int)k;
+        o[0] = r.tMax;
+        o[1] = (float)obj;
+        o[2] = hit ? is.p.x : 0.0f; o[3] = hit ? is.p.y : 0.0f; o[4] = hit ? is.p.z : 0.0f;
+        o[5] = hit ? is.shading.n.x : 0.0f; o[6] = hit ? is.shading.n.y : 0.0f; o[7] = hit ? is.shading.n.z : 0.0f;
+    }
+    return 0;
+}
+
+int xref_intersect_any(void* p, int n, const float* rays, int32_t* out) {
+    RefScene* s = (RefScene*)p;
+    if (!s || !rays || !out || n < 0) return -1;
+    if (!s->built) return -3;
+    for (int i = 0; i < n; ++i) {
+        Ray r(Vector3f(rays[7 * i], rays[7 * i + 1], rays[7 * i + 2]),
+              Vector3f(rays[7 * i + 3], rays[7 * i + 4], rays[7 * i + 5]), rays[7 * i + 6]);
+        out[i] = s->scene.intersectAny(r) ? 1 : 0;
+    }
+    return 0;
+}
+
 int xref_add_material(void* p, int type, const float* f, int base, int tex, int normalmap) {
     RefScene* s = (RefScene*)p;
     std::shared_ptr<Material> m;
@@ -412,7 +447,9 @@ int xref_add_material(void* p, int type, const float* f, int base, int tex, int 
 int xref_add_object(void* p, int mesh, int material, const float* mat, const float* matInv) {
     RefScene* s = (RefScene*)p;
     if (mesh < 0 || mesh >= (int)s->meshes.size() || material < 0 || material >= (int)s->materials.size()) return -1;
-    s->scene.addObject(std::make_shared<Object>(s->meshes[mesh], s->materials[material], toTransform(mat, matInv)));
+    auto obj = std::make_shared<Object>(s->meshes[mesh], s->materials[material], toTransform(mat, matInv));
+    s->objects.push_back(obj.get());
+    s->scene.addObject(obj);
     return 0;
 }
 

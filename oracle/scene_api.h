@@ -28,6 +28,11 @@
  * light_sample_pcg (built scenes only, -3 otherwise): n draws of Scene::sampleSurface
  * (Scene.h:40-47), draw k on the PCG stream (k, 2, seed): out[k] = p.xyz, geometric
  * normal n.xyz, pdf (area measure) (7 floats).
+ *
+ * intersect / intersect_any (built scenes only, -3 otherwise): Scene::intersect and
+ * Scene::intersectAny (Scene.h:30-36) for rays float[n][7] (o, d, tMax):
+ * out[k] = t (the shrunk tMax), object index (-1: miss), p.xyz, shading normal xyz
+ * (8 floats); any-hit: out[k] = 0 / 1.
  */
 #ifndef XGB_ORACLE_SCENE_API_H
 #define XGB_ORACLE_SCENE_API_H
@@ -70,6 +75,8 @@ enum { ORC_INTEGRATOR_STANDARD = 0, ORC_INTEGRATOR_NAIVE = 1 };
     int P##bsdf_eval_pcg(void* s, int material, const float* wo, int n, const float* wi,           \
                          uint32_t seed, float* out);                                               \
     int P##light_sample_pcg(void* s, int n, uint32_t seed, float* out);                            \
+    int P##intersect(void* s, int n, const float* rays, float* out);                               \
+    int P##intersect_any(void* s, int n, const float* rays, int32_t* out);                         \
     int P##add_object(void* s, int mesh, int material, const float* mat, const float* matInv);     \
     int P##set_camera(void* s, const float* c2w, const float* c2wInv, float fov, float aspect);    \
     int P##set_sky(void* s, int type, const float* rgb, int tex);                                  \

@@ -1712,6 +1712,41 @@ int xcpu_render_pcg_aov(void* s, int W, int H, uint32_t spp_begin, uint32_t spp_
                      film, aov, nthreads);
 }
 
+// Scene::intersect / intersectAny for the checkers' known-answer tests (scene_api.h).
+int xcpu_intersect(void* s, int n, const float* rays, float* out) {
+    Scene* sc = (Scene*)s;
+    if (!sc || !rays || !out || n < 0) return -1;
+    if (!sc->built) return -3;
+    for (int i = 0; i < n; ++i) {
+        Ray r;
+        r.o = V3(rays[7 * i], rays[7 * i + 1], rays[7 * i + 2]);
+        r.d = V3(rays[7 * i + 3], rays[7 * i + 4], rays[7 * i + 5]);
+        r.tMax = rays[7 * i + 6];
+        Isect is;
+        float* o = out + 8 * (size_t)i;
+        const bool hit = sceneIntersect(*sc, r, &is);
+        o[0] = r.tMax;
+        o[1] = hit ? (float)is.object : -1.0f;
+        o[2] = hit ? is.p.x : 0.0f; o[3] = hit ? is.p.y : 0.0f; o[4] = hit ? is.p.z : 0.0f;
+        o[5] = hit ? is.sn.x : 0.0f; o[6] = hit ? is.sn.y : 0.0f; o[7] = hit ? is.sn.z : 0.0f;
+    }
+    return 0;
+}
+
+int xcpu_intersect_any(void* s, int n, const float* rays, int32_t* out) {
+    Scene* sc = (Scene*)s;
+    if (!sc || !rays || !out || n < 0) return -1;
+    if (!sc->built) return -3;
+    for (int i = 0; i < n; ++i) {
+        Ray r;
+        r.o = V3(rays[7 * i], rays[7 * i + 1], rays[7 * i + 2]);
+        r.d = V3(rays[7 * i + 3], rays[7 * i + 4], rays[7 * i + 5]);
+        r.tMax = rays[7 * i + 6];
+        out[i] = sceneIntersectAny(*sc, r) ? 1 : 0;
+    }
+    return 0;
+}
+
 // Closest-hit query for traversal known-answer tests: rays are float[n][7]
 // (o, d, tMax); hits are float[n][5] (t, object, triangle, b0, b1), object = -1
 // on a miss. b0/b1 are recomputed by the watertight test on the hit triangle.
