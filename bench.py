@@ -50,9 +50,10 @@ L2_BYTES = 129 * 1024 * 1024
 EXTEND_BYTES_PER_RAY = 52
 # BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
 NODE_BYTES, TRI_BYTES = 64, 48
-# DRAM bytes per extension ray of k_trace_single from one ncu capture of a full
-# 8,388,608-ray launch on the terrain (profiles/trace_single_terrain_ncu.md: 1.501 GB
-# read + 189.3 MB written); scaled to the average launch for roofline.traffic.
+# DRAM bytes per extension ray of k_trace_single (dram__bytes_read.sum +
+# dram__bytes_write.sum over the rays of one launch) from an ncu capture of the
+# terrain workload's extension launch; scaled to the average launch for
+# roofline.traffic.
 EXTEND_DRAM_BYTES_PER_RAY = 201.5
 
 
@@ -84,6 +85,8 @@ def parse():
     p.add_argument("--cpu-sample-res", type=int, default=1024)
     p.add_argument("--cpu-sample-spp", type=int, default=4)
     p.add_argument("--no-guided", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the Cornell, small-batch and reference-defaults measurements after the main line")
     p.add_argument("--guided-res", type=int, default=512)
     p.add_argument("--guided-seconds", type=float, default=8.0)
     p.add_argument("--guided-ref-spp", type=int, default=16384)
@@ -132,6 +135,13 @@ def make_workload(args):
         meta = {"data": "synthetic (the Cornell box of the workload description)", "kernel": FLAT_KERNEL,
                 "l2": "the scene fits in L2 (36 triangles); path queues of 2^23 paths stream through HBM"}
     return desc, label, meta
+
+
+def arm_config(label, meta, world):
+    """The `config` object of both arms' lines (the reference arm runs a bounded
+    sample of this workload and says so outside `config`)."""
+    return {"workload": label, "parallelism": f"replicas x{world} (disjoint sample ranges)", "l2": meta["l2"],
+            "queue_capacity": 1 << 23}
 
 
 class ClockSampler:
@@ -269,8 +279,10 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": meta["data"],
-        "config": {"workload": label, "sample_per_step": f"{res}x{res} film x {spp} spp of the same scene and camera",
-                   "integrator": "reference StandardPathTracer defaults (no depth limit, RR after length 5)"},
+        "config": arm_config(label, meta, 1),
+        "sample_per_step": f"{res}x{res} film x {spp} spp of the same scene and camera",
+        "integrator": ("the reference's StandardPathTracer with its own constants (no depth limit, RR after "
+                       "length 5 at 0.9); the GPU line's reference_defaults entry times the GPU with the same"),
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": nthreads, "kind": kind,
                          "sample": f"{res}x{res}x{spp} per step, {args.steps} steps"},
         "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -302,19 +314,19 @@ def guided_equal_time(ctx, args):
     return out
 
 
-def run_batch(args):
-    """64 independent scenes (seeded soups / heightfields of 1k-500k triangles,
-    films of 128^2-1024^2, 32 spp, max depth 8, 1-4 quad lights) rendered by one
-    xgb_render_batch call per step with autotuned queue size and graph replay,
-    against the same jobs rendered one xgb_render call after another."""
+def batch_measure(ctx, n_scenes, steps, warmup):
+    """The first `n_scenes` scenes of the batch workload (seeded soups / heightfields
+    of 1k-500k triangles, films of 128^2-1024^2, 32 spp, max depth 8, 1-4 quad
+    lights) rendered by one xgb_render_batch call per step with autotuned queue
+    size and graph replay, against the same jobs rendered one xgb_render call
+    after another. Returns the measurement as a dict."""
     import ctypes as C
 
     import torch
 
     from xitils_gb300 import api, scenes
 
-    ctx = api.Context(0)
-    descs = [scenes.batch_scene(i) for i in range(args.batch_scenes)]
+    descs = [scenes.batch_scene(i) for i in range(n_scenes)]
     builders = [api.load_scene(ctx, d) for d in descs]
     targets = [api.RenderTarget(ctx, d.width, d.height) for d in descs]
     paths = sum(d.width * d.height * d.spp for d in descs)
@@ -325,13 +337,13 @@ def run_batch(args):
     t0 = time.perf_counter()
     tuned = api.batch_autotune(ctx, jobs(0))
     t_tune = time.perf_counter() - t0
-    for k in range(args.warmup):
+    for k in range(warmup):
         api.render_batch(ctx, jobs(k))
     ctx.synchronize()
     with ClockSampler(0) as clocks:
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            api.render_batch(ctx, jobs(args.warmup + k))
+        for k in range(steps):
+            api.render_batch(ctx, jobs(warmup + k))
         ctx.synchronize()
         t_batch = time.perf_counter() - t0
     st = api.batch_stats(ctx)
@@ -339,44 +351,90 @@ def run_batch(args):
     hosts = [torch.empty((d.height, d.width, 3), dtype=torch.float32, pin_memory=True).numpy() for d in descs]
     ctx.synchronize()
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        api.render_batch(ctx, jobs(args.warmup + args.steps + k))
+    for k in range(steps):
+        api.render_batch(ctx, jobs(warmup + steps + k))
         for t, h in zip(targets, hosts):
             t.download(h)
     t_e2e = time.perf_counter() - t0
     # the same jobs one render call after another
-    for k in range(1):
-        for d, b, t in zip(descs, builders, targets):
-            t.render(b.scene, d.spp, d.params, 0)
+    for d, b, t in zip(descs, builders, targets):
+        t.render(b.scene, d.spp, d.params, 0)
     ctx.synchronize()
     t0 = time.perf_counter()
-    for k in range(args.steps):
+    for k in range(steps):
         for d, b, t in zip(descs, builders, targets):
-            t.render(b.scene, d.spp, d.params, (args.warmup + k) * d.spp)
+            t.render(b.scene, d.spp, d.params, (warmup + k) * d.spp)
     ctx.synchronize()
     t_seq = time.perf_counter() - t0
-    out = {
-        "metric": "Mpaths/s", "value": paths * args.steps / t_batch / 1e6, "unit": "Mpaths/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_batch / args.steps,
+    return {
+        "metric": "Mpaths/s", "value": paths * steps / t_batch / 1e6, "unit": "Mpaths/s", "n_gpus": 1,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t_batch / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded triangle soups and fBm heightfields)",
         "config": {"workload": f"{len(descs)}-scene batch, {sum(d.n_tris for d in descs)} triangles in all, "
                                f"{paths} paths per step (32 spp each), one xgb_render_batch call per step",
                    "autotuned": tuned, "autotune_seconds": t_tune},
-        "sequential": {"value": paths * args.steps / t_seq / 1e6, "unit": "Mpaths/s",
-                       "ms_per_step": 1e3 * t_seq / args.steps, "how": "one xgb_render call per scene"},
-        "e2e": {"value": paths * args.steps / t_e2e / 1e6, "unit": "Mpaths/s",
+        "sequential": {"value": paths * steps / t_seq / 1e6, "unit": "Mpaths/s",
+                       "ms_per_step": 1e3 * t_seq / steps, "how": "one xgb_render call per scene"},
+        "e2e": {"value": paths * steps / t_e2e / 1e6, "unit": "Mpaths/s",
                 "h2d_bytes_per_step": len(descs) * C.sizeof(api.BatchJobC),
                 "d2h_bytes_per_step": sum(d.width * d.height * 12 for d in descs)},
-        "gpu_launches": st["kernel_launches"] * args.steps,
+        "gpu_launches": st["kernel_launches"] * steps,
         "clocks": clocks.summary(),
         "render_stats": st,
-        "cpu_baseline": None,
-        "timing": "host wall clock around the calls, synchronised (each call ends with a device sync; "
-                  "steps of several seconds)",
+        "timing": "host wall clock around the calls, synchronised (each call ends with a device sync)",
     }
+
+
+def run_batch(args):
+    """The batch workload as the main line (--workload batch)."""
+    from xitils_gb300 import api
+
+    out = batch_measure(api.Context(0), args.batch_scenes, args.steps, args.warmup)
+    out["cpu_baseline"] = None
     print(json.dumps(out))
     return 0
+
+
+def render_measure(ctx, desc, params, steps, warmup, builder=None):
+    """Device time (CUDA events on the render stream) and end-to-end time (the
+    same call plus a film download to pinned host memory) of `steps` render calls
+    of `desc` after `warmup` untimed ones; every call renders new samples."""
+    import ctypes as C
+
+    import torch
+
+    from xitils_gb300 import api
+
+    b = builder or api.load_scene(ctx, desc)
+    W, H, spp = desc.width, desc.height, desc.spp
+    rt = api.RenderTarget(ctx, W, H)
+    stream = torch.cuda.Stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    for k in range(warmup):
+        rt.render(b.scene, spp, params, k * spp, stream=sptr)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(steps):
+        rt.render(b.scene, spp, params, (warmup + k) * spp, stream=sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    err = b.scene.stats(stream=sptr)["error_flags"]
+    host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True).numpy()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        rt.render(b.scene, spp, params, (warmup + steps + k) * spp, stream=sptr)
+        rt.download(host, stream=sptr)
+    t_e2e = time.perf_counter() - t0
+    paths = W * H * spp * steps
+    return {"value": paths / (ms / 1e3) / 1e6, "unit": "Mpaths/s", "ms_per_step": ms / steps, "steps": steps,
+            "warmup": warmup,
+            "e2e": {"value": paths / t_e2e / 1e6, "unit": "Mpaths/s",
+                    "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC), "d2h_bytes_per_step": W * H * 12},
+            "error_flags": err}
 
 
 def run_mfnm(args):
@@ -513,6 +571,9 @@ def run_xgb(args):
 
     agg = {k: sum(s[k] for s in stats) for k in ("paths", "extension_rays", "shadow_rays", "iterations",
                                                    "kernel_launches", "node_visits", "tri_tests")}
+    agg["error_flags"] = 0
+    for s_ in stats:
+        agg["error_flags"] |= s_["error_flags"]
     stage_ms = [sum(s["kernel_ms"][j] for s in stats) for j in range(5)]
     stage_launch = [sum(s["stage_launches"][j] for s in stats) for j in range(5)]
     pk = peaks()
@@ -531,8 +592,8 @@ def run_xgb(args):
         # the DRAM bytes per ray come from the terrain's ncu capture; other workloads have none
         "traffic": (EXTEND_DRAM_BYTES_PER_RAY * agg["extension_rays"] / ext_launches
                     if args.workload == "terrain" else None),
-        "traffic_source": ("ncu dram__bytes_read+write per ray (profiles/trace_single_terrain_ncu.md) x rays per launch"
-                           if args.workload == "terrain" else "no ncu capture of this workload"),
+        "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per ray of a terrain extension launch "
+                           "x rays per launch" if args.workload == "terrain" else "no ncu capture of this workload"),
         "algorithmic_bytes_per_launch": EXTEND_BYTES_PER_RAY * agg["extension_rays"] / ext_launches,
         "avg_launch_ms": ext_ms / ext_launches,
         "bvh_l2_gbs": ((NODE_BYTES * agg["node_visits"] + TRI_BYTES * agg["tri_tests"]) / (ext_ms / 1e3) / 1e9
@@ -562,6 +623,20 @@ def run_xgb(args):
         except Exception as e:
             cpu = {"value": None, "unit": "Mpaths/s", "cores": os.cpu_count(), "kind": "reference",
                    "sample": f"unavailable: {e}"}
+    extras = {}
+    if not args.no_extras and world == 1:
+        from xitils_gb300 import scenes
+        from xitils_gb300.scene import IntegratorParams
+        if args.workload == "terrain":
+            m = render_measure(ctx, desc, IntegratorParams(seed=desc.params.seed), args.steps, 3, builder=builder)
+            m["config"] = dict(arm_config(label.replace("max depth 10", "reference integrator defaults"), meta, 1),
+                               integrator="no depth limit, RR after length 5 at 0.9 (the reference arm's settings)")
+            extras["reference_defaults"] = m
+        c1 = scenes.cornell(512, 512, 16)
+        m = render_measure(ctx, c1, c1.params, args.steps, 3)
+        m["config"] = {"workload": "cornell 36 tris, 512x512 film, 16 spp, max depth 8, RR after depth 3"}
+        extras["cornell"] = m
+        extras["batch"] = batch_measure(ctx, 16, 3, 1)
     guided = None
     if not args.no_guided and world == 1:
         try:
@@ -574,9 +649,7 @@ def run_xgb(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": meta["data"],
-        "config": {"workload": label, "parallelism": f"replicas x{world} (disjoint sample ranges)",
-                   "l2": meta["l2"],
-                   "queue_capacity": 1 << 23},
+        "config": arm_config(label, meta, world),
         "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": C.sizeof(api.IntegratorParamsC),
                 "d2h_bytes_per_step": W * H * 12},
         "gpu_launches": agg["kernel_launches"] // len(stats) * args.steps,
@@ -590,6 +663,7 @@ def run_xgb(args):
         "render_stats": agg,
         "guided_equal_time": guided,
     }
+    out.update(extras)
     if svndf_fit is not None:
         out["svndf_fit"] = svndf_fit
     print(json.dumps(out))

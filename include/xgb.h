@@ -272,7 +272,7 @@ typedef struct {
     uint64_t kernel_launches;/* kernels launched by the call */
     uint64_t node_visits;    /* BVH nodes visited by extension rays (profiling only) */
     uint64_t tri_tests;      /* triangle tests of extension rays (profiling only) */
-    uint32_t error_flags;    /* device error bits: 1 traversal stack overflow */
+    uint32_t error_flags;    /* device error bits: 1 traversal stack overflow, 4 traversal step bound */
     uint32_t profiled;       /* 1 when the timings below were recorded */
     /* summed device time per kernel stage, CUDA events on the render stream:
        [0] plan, [1] generate, [2] extend (closest hit), [3] shade, [4] shadow (any hit) */
@@ -324,10 +324,13 @@ xgb_status xgb_render_stats_get(xgb_scene* scene, xgb_render_stats* out, void* s
  * are in flight: params->queue_capacity above that returns XGB_INVALID_ARG
  * (0 = the maximum); sample counts are not limited. Every call shares the array
  * and re-initialises its counters, so calls whose GPU work overlaps (other
- * streams or threads) race and must be serialised. The first call on a device
- * looks up the array's address: make it before any stream capture. Errors are
- * reported through the return code only (the context's error text is not
- * touched). */
+ * streams or threads) race and must be serialised. Every call looks up the
+ * array's address with the scene's device current (cudaGetSymbolAddress, no
+ * allocation): make the first call on a device before any stream capture.
+ * Radiance only: a film with AOV planes or a scene with a learned proposal
+ * returns XGB_UNSUPPORTED (both need per-call device memory), and the scene's
+ * xgb_render_stats_get counters are not updated. Errors are reported through
+ * the return code only (the context's error text is not touched). */
 #define XGB_NOALLOC_MAX_PATHS 32768
 xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_params* params, xgb_film* film,
                               uint32_t spp_begin, uint32_t spp_count, void* stream);
@@ -394,6 +397,20 @@ xgb_status xgb_scene_set_fixes(xgb_scene* scene, uint32_t fixes);
  * within tMax, else 0. Synchronises the stream. */
 xgb_status xgb_scene_intersect(xgb_scene* scene, int n, const float* rays, float* hits, void* stream);
 xgb_status xgb_scene_occluded(xgb_scene* scene, int n, const float* rays, int32_t* occluded, void* stream);
+
+/* Device-side bounds of ray traversal on this scene (no counterpart in the
+ * reference, whose recursive traversal has none): a ray that takes more than
+ * max_steps traversal loop steps ends and the render returns
+ * XGB_DEVICE_TIMEOUT; a ray whose traversal would push onto a stack already
+ * holding max_stack entries ends and the render returns XGB_QUEUE_OVERFLOW.
+ * Either way the film is incomplete, the error bit is in
+ * xgb_render_stats.error_flags (4 and 1), the context stays usable and the
+ * next call starts with clear bits. 0 restores a default: 2^22 steps, 64
+ * entries (the stacks' size; max_stack above 64 is XGB_INVALID_ARG). A
+ * well-formed BVH never reaches the defaults; lower values are for testing
+ * the error paths. Applies to xgb_render, xgb_render_batch,
+ * xgb_render_noalloc and the ray queries on this scene. */
+xgb_status xgb_scene_set_traversal_limits(xgb_scene* scene, int max_steps, int max_stack);
 
 /* enable = 1: later xgb_render calls on this scene record CUDA events around
  * every kernel on the render stream and count BVH work (for profiling; adds a

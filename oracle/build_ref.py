@@ -46,7 +46,10 @@ ORACLE_SO = os.path.join(HERE, "liboracle.so")
 ORACLE_PERTURBED_SO = os.path.join(HERE, "liboracle_ulp.so")
 REF_SO = os.path.join(REF_OUT, "libxref.so")
 
-REFERENCE_ROOT = os.environ.get("XGB_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: XGB_REFERENCE_ROOT, else a sibling directory of the
+# repository named "reference".
+REFERENCE_ROOT = os.environ.get("XGB_REFERENCE_ROOT",
+                                os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 HEADERS = [
     "AccelerationStructure.h", "Bounds.h", "Camera.h", "Geometry.h", "Interaction.h", "Material.h",
     "Matrix.h", "Object.h", "PathTracer.h", "Ray.h", "RenderTarget.h", "Sampler.h", "Scene.h",

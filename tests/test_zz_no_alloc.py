@@ -17,6 +17,7 @@ from xitils_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 XGB_INVALID_ARG = 1
+XGB_UNSUPPORTED = 7
 MAX_PATHS = 32768
 
 
@@ -70,4 +71,13 @@ def test_noalloc_rejects_capacity_beyond_maximum(setup):
     film = api.RenderTarget(ctx, desc.width, desc.height)
     pc = _params(api, desc, MAX_PATHS + 1)
     assert ctx.lib.xgb_render_noalloc(builder.scene.h, C.byref(pc), film.h, 0, 1, None) == XGB_INVALID_ARG
+    assert film.download().sum() == 0.0
+
+
+def test_noalloc_refuses_what_needs_per_call_memory(setup):
+    """AOV planes and a learned proposal need device memory per call: refused, film untouched."""
+    api, ctx, desc, builder = setup
+    film = api.RenderTarget(ctx, desc.width, desc.height, aovs=True)
+    pc = _params(api, desc)
+    assert ctx.lib.xgb_render_noalloc(builder.scene.h, C.byref(pc), film.h, 0, 1, None) == XGB_UNSUPPORTED
     assert film.download().sum() == 0.0

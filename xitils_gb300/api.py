@@ -127,6 +127,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_batch_autotune": [C.POINTER(BatchJobC), C.c_int, P, C.POINTER(BatchOptionsC)],
         "xgb_batch_stats_get": [P, C.POINTER(RenderStatsC)],
         "xgb_scene_set_profiling": [P, C.c_int],
+        "xgb_scene_set_traversal_limits": [P, C.c_int, C.c_int],
         "xgb_render_noalloc": [P, C.POINTER(IntegratorParamsC), P, C.c_uint32, C.c_uint32, P],
         "xgb_guide_create": [P, C.c_uint32, C.POINTER(P)],
         "xgb_guide_destroy": [P],
@@ -477,6 +478,11 @@ class Scene:
 
     def set_profiling(self, enable: bool = True):
         self.ctx.check(self.ctx.lib.xgb_scene_set_profiling(self.h, int(enable)), "set_profiling")
+
+    def set_traversal_limits(self, max_steps: int = 0, max_stack: int = 0):
+        """Device-side traversal bounds (0 = default: 2^22 steps, 64 stack entries)."""
+        self.ctx.check(self.ctx.lib.xgb_scene_set_traversal_limits(self.h, int(max_steps), int(max_stack)),
+                       "set_traversal_limits")
 
     def stats(self, stream=None) -> dict:
         s = RenderStatsC()

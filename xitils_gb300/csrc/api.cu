@@ -146,6 +146,7 @@ struct xgb_film {
     int w = 0, h = 0, fp64 = 0;
     void* d = nullptr;
     void* aov = nullptr;  // albedo plane then normal plane, same element type as d
+    float* stage = nullptr;  // packed float RGB(A) of one plane for downloads (allocated at the first one)
 };
 
 struct xgb_guide {
@@ -204,6 +205,8 @@ struct xgb_scene {
     float4* mix = nullptr;  // per-path mixtures (capacity x 10 float4)
     unsigned int mixCapacity = 0;
     unsigned int fixes = 0;     // opt-in quirk fixes (xgb_scene_set_fixes)
+    int maxSteps = kDefaultMaxSteps;   // traversal bounds (xgb_scene_set_traversal_limits)
+    int stackLimit = kMaxStackLimit;
     bool guidable = false;      // some object's material takes the learned proposal
     float4* pathAcc = nullptr;  // guide training: per-path contributions of a call
     unsigned long long pathAccCapacity = 0;
@@ -1047,6 +1050,8 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.tlasRootIsLeaf = tlasRootIsLeaf;
     sd.blasLayout = blasLayout;
     sd.fixes = (int)s->fixes;
+    sd.maxSteps = s->maxSteps;
+    sd.stackLimit = s->stackLimit;
     sd.shell = anyShell;
     sd.nested = 0;
     for (const Material& m : dm) sd.nested |= (m.kind == MAT_MF_NORMALMAP ? 1 : 0) | (m.kind == MAT_MULTILOBE_SVBRDF ? 2 : 0);
@@ -1089,6 +1094,7 @@ xgb_status xgb_film_destroy(xgb_film* f) {
     if (!f) return XGB_INVALID_ARG;
     dfree(f->d);
     dfree(f->aov);
+    dfree(f->stage);
     delete f;
     return XGB_OK;
 }
@@ -1099,22 +1105,25 @@ xgb_status xgb_film_clear(xgb_film* f, void* stream) {
     if (f->aov) XGB_CUDA(f->ctx, cudaMemsetAsync(f->aov, 0, 2 * filmPlaneBytes(f), pick(f->ctx, stream)));
     return XGB_OK;
 }
+// A plane to host floats: a kernel packs it (FP64 rounded to float, the
+// caller's 12- or 16-byte pixel stride) into the film's staging buffer, and one
+// linear copy moves it to the host pointer (pinned or pageable).
 static xgb_status downloadPlane(xgb_film* f, const void* src, float* host, int stride, cudaStream_t st) {
-    size_t n = (size_t)f->w * f->h;
-    const int fs = stride / 4;
-    if (f->fp64) {
-        std::vector<double> tmp(4 * n);
-        XGB_CUDA(f->ctx, cudaMemcpyAsync(tmp.data(), src, 32 * n, cudaMemcpyDeviceToHost, st));
-        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
-        for (size_t i = 0; i < n; ++i)
-            for (int k = 0; k < 3; ++k) host[fs * i + k] = (float)tmp[4 * i + k];
-    } else if (stride == 16) {
-        XGB_CUDA(f->ctx, cudaMemcpyAsync(host, src, 16 * n, cudaMemcpyDeviceToHost, st));
-        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
-    } else {
-        XGB_CUDA(f->ctx, cudaMemcpy2DAsync(host, 12, src, 16, 12, n, cudaMemcpyDeviceToHost, st));
-        XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
+    const size_t n = (size_t)f->w * f->h;
+    cudaSetDevice(f->ctx->device);
+    if (!f->stage) {
+        cudaError_t e = cudaMalloc((void**)&f->stage, 16 * n);
+        if (e != cudaSuccess) {
+            f->stage = nullptr;
+            return e == cudaErrorMemoryAllocation ? fail(f->ctx, XGB_OOM, "xgb_film_download: out of memory")
+                                                  : cudaFail(f->ctx, e, "xgb_film_download");
+        }
     }
+    const int grid = f->ctx->numSMs * 8;
+    launchPackFilm(src, f->fp64, n, stride / 4, f->stage, grid, st);
+    XGB_CUDA(f->ctx, cudaGetLastError());
+    XGB_CUDA(f->ctx, cudaMemcpyAsync(host, f->stage, (size_t)stride * n, cudaMemcpyDeviceToHost, st));
+    XGB_CUDA(f->ctx, cudaStreamSynchronize(st));
     return XGB_OK;
 }
 xgb_status xgb_film_download(xgb_film* f, float* host, int stride, void* stream) {
@@ -1440,6 +1449,17 @@ xgb_status xgb_scene_set_fixes(xgb_scene* s, uint32_t fixes) {
     return XGB_OK;
 }
 
+xgb_status xgb_scene_set_traversal_limits(xgb_scene* s, int max_steps, int max_stack) {
+    if (!s) return XGB_INVALID_ARG;
+    if (max_steps < 0 || max_stack < 0 || max_stack > kMaxStackLimit)
+        return fail(s->ctx, XGB_INVALID_ARG, "xgb_scene_set_traversal_limits: max_steps >= 0, max_stack in [0, 64]");
+    s->maxSteps = max_steps ? max_steps : kDefaultMaxSteps;
+    s->stackLimit = max_stack ? max_stack : kMaxStackLimit;
+    s->sd.maxSteps = s->maxSteps;
+    s->sd.stackLimit = s->stackLimit;
+    return XGB_OK;
+}
+
 xgb_status xgb_scene_set_profiling(xgb_scene* s, int enable) {
     if (!s) return XGB_INVALID_ARG;
     s->profiling = enable != 0;
@@ -1474,6 +1494,12 @@ bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp
     *h = f->h;
     *fp64 = f->fp64;
     return true;
+}
+// What xgb_render would add beyond the plain radiance: AOV planes on the film, a
+// learned proposal on the scene.
+void renderExtras(const xgb_scene* s, const xgb_film* f, int* filmAovs, int* sceneGuide) {
+    *filmAovs = (f && f->aov) ? 1 : 0;
+    *sceneGuide = (s && s->guide) ? 1 : 0;
 }
 xgb_ctx* sceneContext(xgb_scene* s) { return s ? s->ctx : nullptr; }
 xgb_status contextFail(xgb_ctx* ctx, xgb_status st, const std::string& msg) { return fail(ctx, st, msg); }

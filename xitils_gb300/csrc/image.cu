@@ -44,6 +44,29 @@ __global__ void k_tonemap(const void* film, int fp64, size_t n, float scale, flo
         }
 }
 
+// Film plane -> packed float RGB with `stride` floats per pixel (3 or 4), FP64
+// films rounded to float: one linear device-to-host copy then moves the result
+// (a strided 2D copy of 12-byte rows is slow on the copy engines).
+__global__ void k_packFilm(const void* film, int fp64, size_t n, int stride, float* out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float r, g, b, w;
+        if (fp64) {
+            const double4 v = ((const double4*)film)[i];
+            r = (float)v.x; g = (float)v.y; b = (float)v.z; w = (float)v.w;
+        } else {
+            const float4 v = __ldcs((const float4*)film + i);
+            r = v.x; g = v.y; b = v.z; w = v.w;
+        }
+        if (stride == 4) {
+            __stcs((float4*)out + i, make_float4(r, g, b, w));
+        } else {
+            out[3 * i] = r;
+            out[3 * i + 1] = g;
+            out[3 * i + 2] = b;
+        }
+    }
+}
+
 __device__ __forceinline__ float lum(float r, float g, float b) { return 0.298912f * r + 0.586611f * g + 0.114478f * b; }
 
 __device__ __forceinline__ float jet(float t, float m) { return fminf(fmaxf(1.5f - 4.0f * fabsf(t - m), 0.0f), 1.0f); }
@@ -92,6 +115,10 @@ void chunk(std::vector<unsigned char>& out, const Crc& crc, const char* type, co
 }
 
 }  // namespace
+
+void launchPackFilm(const void* film, int fp64, size_t n, int strideFloats, float* out, int grid, cudaStream_t s) {
+    k_packFilm<<<grid, 256, 0, s>>>(film, fp64, n, strideFloats, out);
+}
 }  // namespace xgb
 
 using namespace xgb;

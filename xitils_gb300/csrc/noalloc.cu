@@ -21,11 +21,15 @@
 //  * all calls share the one array per device and every call re-initialises the
 //    counters it needs; calls whose GPU work overlaps (other streams, other host
 //    threads) race on it and must be serialised by the caller.
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture.
+//  * every call looks up the array's device address (cudaGetSymbolAddress,
+//    with the scene's device current), so the address stays right after a
+//    context reset; make the first call on a device before any stream capture.
+//  * the film receives the radiance only: a film with AOV planes
+//    (xgb_film_enable_aovs) or a scene with a learned proposal
+//    (xgb_scene_set_guide) is refused with XGB_UNSUPPORTED, since both need
+//    per-call device memory. The scene's last-render statistics
+//    (xgb_render_stats_get) are not updated.
 #include <cstring>
-#include <mutex>
 
 #include "../../include/xgb.h"
 #include "xgb_kernels.h"
@@ -33,6 +37,7 @@
 namespace xgb {
 bool sceneView(xgb_scene* s, SceneDev* sd, int* device, int* numSMs, cudaStream_t* stream, int* built);
 bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp64);
+void renderExtras(const xgb_scene* s, const xgb_film* f, int* filmAovs, int* sceneGuide);
 }  // namespace xgb
 
 using namespace xgb;
@@ -50,7 +55,6 @@ constexpr size_t kScratchBytes = 2 * kQueueBytes      // path queues (in, out)
                                  + kV4 + kI1          // hit records
                                  + 3 * kV4 + kU2      // shadow queue
                                  + up(sizeof(Ctrl));  // counters
-constexpr int kMaxDevices = 64;
 
 }  // namespace
 
@@ -59,19 +63,15 @@ static __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
 
 namespace {
 
-std::mutex g_setupMutex;
-unsigned char* g_scratchAddr[kMaxDevices] = {};
-
-// Device address of g_noallocScratch for `device` (current). Once per device.
-cudaError_t scratchFor(int device, unsigned char** out) {
-    std::lock_guard<std::mutex> lock(g_setupMutex);
-    if (!g_scratchAddr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
-        if (e != cudaSuccess) return e;
-        g_scratchAddr[device] = (unsigned char*)p;
-    }
-    *out = g_scratchAddr[device];
+// Device address of g_noallocScratch on the current device. In host code the
+// array's name is only a host-side stand-in, never a device address; the
+// lookup allocates nothing and is repeated on every call, so a context
+// recreated by the host application (cudaDeviceReset) is picked up.
+cudaError_t scratchAddress(unsigned char** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    if (e != cudaSuccess) return e;
+    *out = (unsigned char*)p;
     return cudaSuccess;
 }
 
@@ -87,6 +87,9 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     void* filmPtr = nullptr;
     int W = 0, H = 0, fp64 = 0;
     if (!filmView(film, scene, &filmPtr, &W, &H, &fp64)) return XGB_INVALID_ARG;
+    int filmAovs = 0, sceneGuide = 0;
+    renderExtras(scene, film, &filmAovs, &sceneGuide);
+    if (filmAovs || sceneGuide) return XGB_UNSUPPORTED;
     xgb_integrator_params P;
     if (params) P = *params;
     else xgb_integrator_params_default(&P);
@@ -95,7 +98,6 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
         return XGB_INVALID_ARG;
     if (P.max_depth == 0 && P.rr_prob >= 1.0f) return XGB_INVALID_ARG;
     if (P.queue_capacity < 0 || (unsigned int)P.queue_capacity > kNoAllocMaxPaths) return XGB_INVALID_ARG;
-    if (device < 0 || device >= kMaxDevices) return XGB_UNSUPPORTED;
     if (cudaSetDevice(device) != cudaSuccess) return XGB_CUDA_ERROR;
     cudaStream_t st = stream ? (cudaStream_t)stream : ctxStream;
     unsigned long long total = (unsigned long long)W * H * spp_count;
@@ -103,20 +105,20 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     const unsigned int cap = P.queue_capacity > 0 ? (unsigned int)P.queue_capacity : kNoAllocMaxPaths;
 
     unsigned char* base = nullptr;
-    if (scratchFor(device, &base) != cudaSuccess) return XGB_CUDA_ERROR;
+    if (scratchAddress(&base) != cudaSuccess) return XGB_CUDA_ERROR;
     unsigned char* p = base;
     auto take = [&](size_t bytes) { unsigned char* r = p; p += bytes; return r; };
-    PathQueue q[2];
+    PathQueue q[2]{};  // training fields (grec, pid) stay null: guiding is refused above
     for (int k = 0; k < 2; ++k) {
         q[k].o = (float4*)take(kV4);
         q[k].d = (float4*)take(kV4);
         q[k].thr = (float4*)take(kV4);
         q[k].rng = (uint2*)take(kU2);
     }
-    HitQueue hits;
+    HitQueue hits{};
     hits.h = (float4*)take(kV4);
     hits.inst = (int*)take(kI1);
-    ShadowQueue sq;
+    ShadowQueue sq{};
     sq.o = (float4*)take(kV4);
     sq.d = (float4*)take(kV4);
     sq.c = (float4*)take(kV4);

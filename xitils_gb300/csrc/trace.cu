@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
             const bool active = inMesh && leafCnt == 0;
             if (!__any_sync(__activemask(), active)) break;
             if (!active) continue;
-            if (++steps > kMaxVisits) {
+            if (++steps > sc.maxSteps) {
                 atomicOr(&ctrl->errors, 4u);
                 inMesh = false;
                 inst = nInst;
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_wide(SceneDev sc, RenderP
             const unsigned int mb = byteOf(slot >> 2 ? hd.meta1 : hd.meta0, slot);
             if ((hd.imask >> slot) & 1u) {
                 if (mask) {
-                    if (sp >= kWideStack) {
+                    if (sp >= kWideStack || sp >= sc.stackLimit) {
                         atomicOr(&ctrl->errors, 1u);
                         inMesh = false;
                         inst = nInst;
@@ -417,7 +417,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > kMaxVisits) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; inst = nInst; }
+        if (guard > scenes.scene(job).maxSteps) {
+            atomicOr(&ctrl->errors, 4u);
+            nodeAddr = kSentinel;
+            leafAddr = 0;
+            inst = nInst;
+        }
         bool searching = true;
         while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
             if (COUNT) wc.nodes++;
@@ -430,7 +435,12 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= kStackDepth) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
+                if (sp >= kStackDepth || sp >= scenes.scene(job).stackLimit) {
+                    atomicOr(&ctrl->errors, 1u);
+                    sp = 0;
+                    nodeAddr = kSentinel;
+                    break;
+                }
                 stack[sp++] = far;
                 nodeAddr = near;
             } else if (h0) {
@@ -546,7 +556,7 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > kMaxVisits) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
+        if (guard > sc.maxSteps) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
         bool searching = true;
         while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
             if (COUNT) wc.nodes++;
@@ -559,7 +569,7 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= kStackDepth) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
+                if (sp >= sc.stackLimit) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
                 stack[sp++] = far;
                 nodeAddr = near;
             } else if (h0) {

@@ -16,10 +16,17 @@
 
 namespace xgb {
 
-constexpr int kStackDepth = 64;  // binary top-level traversal
-// Upper bound on loop iterations of one traversal; a well-formed BVH never
-// comes close. Exceeding it sets error bit 4 and ends the traversal.
-constexpr int kMaxVisits = 1 << 22;
+constexpr int kStackDepth = kMaxStackLimit;  // binary mesh traversal
+constexpr int kTlasStack = 16;                // top level over instances
+// Loop iterations of one traversal are bounded by SceneDev::maxSteps (a
+// well-formed BVH never comes close to the default, 2^22); exceeding it sets
+// error bit 4 and ends the traversal. Stack pushes are bounded by
+// SceneDev::stackLimit (at most the stacks' size); exceeding it sets error
+// bit 1 and ends the traversal.
+struct Limits {
+    int steps, stack;
+};
+__device__ __forceinline__ Limits limitsOf(const SceneDev& sc) { return Limits{sc.maxSteps, sc.stackLimit}; }
 
 struct TraceHit {
     float t, b0, b1;
@@ -279,13 +286,13 @@ __device__ __forceinline__ bool testTrisMesh(const MeshDev& m, int first, int cn
 // Traverses one binary mesh BVH (Node2). ANY: returns at the first accepted hit.
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool traverseBlas2(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
-                                             unsigned int* errors, WorkCount& wc) {
+                                             unsigned int* errors, WorkCount& wc, Limits lim) {
     int stack[kStackDepth];
     int sp = 0;
     int node = m.rootIsLeaf ? m.rootLeaf : 0;
     bool found = false;
     for (int guard = 0;; ++guard) {
-        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (guard > lim.steps) { atomicOr(errors, 4u); return found; }
         if (node >= 0) {
             if (COUNT) wc.nodes++;
             const Node2* nd = m.nodes2 + node;
@@ -297,7 +304,7 @@ __device__ __forceinline__ bool traverseBlas2(const MeshDev& m, const WRay& r, f
             if (h0 && h1) {
                 int near = d.x, far = d.y;
                 if (t1 < t0) { near = d.y; far = d.x; }
-                if (sp >= kStackDepth) { atomicOr(errors, 1u); return found; }
+                if (sp >= lim.stack) { atomicOr(errors, 1u); return found; }
                 stack[sp++] = far;
                 node = near;
             } else if (h0) {
@@ -335,7 +342,7 @@ __device__ __forceinline__ bool traverseBlas2(const MeshDev& m, const WRay& r, f
 // Traverses one 8-wide mesh BVH (WNode). ANY: returns at the first accepted hit.
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
-                                                 unsigned int* errors, WorkCount& wc) {
+                                                 unsigned int* errors, WorkCount& wc, Limits lim) {
     if (m.rootIsLeaf) {
         if (COUNT) wc.tris += m.nTris;
         return testTrisMesh<ANY>(m, 0, m.nTris, r, tMax, hit, inst);
@@ -348,8 +355,9 @@ __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r
     unsigned int mask = wideEval(m.nodes, r, oct, tMax, h);
     if (COUNT) wc.nodes++;
     bool found = false;
+    const int stackCap = lim.stack < kWideStack ? lim.stack : kWideStack;
     for (int guard = 0;; ++guard) {
-        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (guard > lim.steps) { atomicOr(errors, 4u); return found; }
         if (mask == 0u) {
             if (sp == 0) break;
             const unsigned int e = stack[--sp];
@@ -363,7 +371,7 @@ __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r
         const unsigned int mb = byteOf(slot >> 2 ? h.meta1 : h.meta0, slot);
         if ((h.imask >> slot) & 1u) {
             if (mask) {
-                if (sp >= kWideStack) { atomicOr(errors, 1u); return found; }
+                if (sp >= stackCap) { atomicOr(errors, 1u); return found; }
                 stack[sp++] = ((unsigned int)node << 8) | mask;
             }
             node = h.childBase + (int)mb;
@@ -383,9 +391,9 @@ __device__ __forceinline__ bool traverseBlasWide(const MeshDev& m, const WRay& r
 
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool traverseBlas(const MeshDev& m, const WRay& r, float& tMax, TraceHit& hit, int inst,
-                                             unsigned int* errors, WorkCount& wc) {
-    return m.wide ? traverseBlasWide<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc)
-                  : traverseBlas2<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc);
+                                             unsigned int* errors, WorkCount& wc, Limits lim) {
+    return m.wide ? traverseBlasWide<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc, lim)
+                  : traverseBlas2<ANY, COUNT>(m, r, tMax, hit, inst, errors, wc, lim);
 }
 
 // Scene::intersect (ANY = false) / Scene::intersectAny (ANY = true).
@@ -396,12 +404,14 @@ __device__ __forceinline__ bool traceScene(const SceneDev& sc, V3 o, V3 d, float
     hit.inst = -1;
     hit.t = tMax;
     WRay wr = makeWRay(o, d);
-    int stack[16];
+    const Limits lim = limitsOf(sc);
+    const int stackCap = lim.stack < kTlasStack ? lim.stack : kTlasStack;
+    int stack[kTlasStack];
     int sp = 0;
     int node = sc.tlasRootIsLeaf ? leafEncode(0, 1) : 0;
     bool found = false;
     for (int guard = 0;; ++guard) {
-        if (guard > kMaxVisits) { atomicOr(errors, 4u); return found; }
+        if (guard > lim.steps) { atomicOr(errors, 4u); return found; }
         if (node >= 0) {
             if (COUNT) wc.nodes++;
             const Node2* nd = sc.tlas + node;
@@ -413,7 +423,7 @@ __device__ __forceinline__ bool traceScene(const SceneDev& sc, V3 o, V3 d, float
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= 16) { atomicOr(errors, 1u); return found; }
+                if (sp >= stackCap) { atomicOr(errors, 1u); return found; }
                 stack[sp++] = far;
                 node = near;
             } else if (h0) {
@@ -430,12 +440,12 @@ __device__ __forceinline__ bool traceScene(const SceneDev& sc, V3 o, V3 d, float
             const MeshDev& m = sc.meshes[in.mesh];
             bool h;
             if (in.identity) {
-                h = traverseBlas<ANY, COUNT>(m, wr, tMax, hit, inst, errors, wc);
+                h = traverseBlas<ANY, COUNT>(m, wr, tMax, hit, inst, errors, wc, lim);
             } else {
                 V3 oo = xformPointRn(in.matInv, o);
                 V3 od = xformVectorRn(in.matInv, d);
                 WRay orr = makeWRay(oo, od);
-                h = traverseBlas<ANY, COUNT>(m, orr, tMax, hit, inst, errors, wc);
+                h = traverseBlas<ANY, COUNT>(m, orr, tMax, hit, inst, errors, wc, lim);
             }
             if (h) {
                 found = true;

@@ -157,6 +157,8 @@ void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQu
                  Ctrl* ctrl, int numSMs, cudaStream_t s);
 void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs,
                   cudaStream_t s);
+// Film plane (float4 or double4 per pixel) -> packed float RGB, strideFloats 3 or 4 (image.cu).
+void launchPackFilm(const void* film, int fp64, size_t n, int strideFloats, float* out, int grid, cudaStream_t s);
 // Ray queries on a built scene: rays o (xyz, w = tMax) and d; closest hits as 2 float4
 // per ray (t, bits(instance), bits(triangle), -; b0, b1, -, -) or any-hit flags.
 void launchQuery(const SceneDev& sc, const float4* o, const float4* d, int n, int any, float4* hits, int* occluded,

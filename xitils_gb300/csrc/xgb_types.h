@@ -149,6 +149,9 @@ struct LightDev {
     int triOffset;
 };
 
+constexpr int kDefaultMaxSteps = 1 << 22;
+constexpr int kMaxStackLimit = 64;
+
 struct SceneDev {
     const MeshDev* meshes;
     const Instance* instances;
@@ -159,6 +162,12 @@ struct SceneDev {
     int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
     int shell;       // 1 when some mesh is shell-mapped (its hits can be discarded during traversal)
     int nested;      // materials that evaluate another: bit 0 microfacet normal mapping, bit 1 MultiLobeSVBRDF
+    // Device-side traversal bounds (xgb_scene_set_traversal_limits): a ray whose
+    // traversal takes more than maxSteps loop steps sets error bit 4 and ends; a
+    // push onto a stack already holding stackLimit entries sets error bit 1 and
+    // ends the ray. Defaults: kDefaultMaxSteps and 64 (the stacks' size).
+    int maxSteps;
+    int stackLimit;
     const float4* instBox;  // per instance: world box lo (xyz), hi (xyz) as 2 float4
     const Material* materials;
     const TextureDev* textures;
