@@ -31,6 +31,8 @@ class CpuChecker:
             path, prefix = build_ref.build_oracle(), "xcpu_"
         elif kind == "port_ulp":
             path, prefix = build_ref.build_oracle_perturbed(), "xcpu_"
+        elif kind.startswith("port_cr"):
+            path, prefix = build_ref.build_oracle_cr(int(kind[len("port_cr"):])), "xcpu_"
         elif kind == "reference":
             path, prefix = build_ref.build_ref(), "xref_"
             if path is None:

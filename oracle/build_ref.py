@@ -131,6 +131,18 @@ def build_oracle_perturbed(force: bool = False) -> str:
     return ORACLE_PERTURBED_SO
 
 
+def build_oracle_cr(mask: int, force: bool = False) -> str:
+    """The oracle with the float functions of `mask` correctly rounded (1 sinf,
+    2 cosf, 4 powf, 8 expf, 16 logf, 32 asinf, 64 acosf, 128 atan2f; computed in
+    long double): a diagnostic that measures what the C library's misrounded
+    results contribute to an image."""
+    src = os.path.join(HERE, "xgb_cpu.cpp")
+    out = os.path.join(HERE, f"liboracle_cr{mask}.so")
+    if force or not os.path.exists(out) or os.path.getmtime(src) > os.path.getmtime(out):
+        _compile(src, out, [HERE], "c++17", (f"XGB_ORACLE_CR={mask}",))
+    return out
+
+
 def build_ref(force: bool = False) -> str | None:
     """Build oracle/_ref/libxref.so when staged sources exist. Returns the path
     or None when neither the reference checkout nor a staged copy is present."""

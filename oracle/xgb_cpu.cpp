@@ -50,6 +50,35 @@ inline float perturbedAsin(float x) { return towardZero(std::asin(x)); }
 #define asinf perturbedAsin
 #endif
 
+#ifdef XGB_ORACLE_CR
+// Diagnostic variant (tests only): the float functions selected by the bit mask
+// XGB_ORACLE_CR (1 sinf, 2 cosf, 4 powf, 8 expf, 16 logf, 32 asinf, 64 acosf,
+// 128 atan2f) return the correctly rounded result, computed in long double and
+// rounded once to float, instead of the C library's. Comparing this build with
+// the plain one measures how much each library function's misrounded results
+// move an image.
+inline float crSin(float x) { return (XGB_ORACLE_CR & 1) ? (float)sinl((long double)x) : std::sin(x); }
+inline float crCos(float x) { return (XGB_ORACLE_CR & 2) ? (float)cosl((long double)x) : std::cos(x); }
+inline float crPow(float x, float y) {
+    return (XGB_ORACLE_CR & 4) ? (float)powl((long double)x, (long double)y) : std::pow(x, y);
+}
+inline float crExp(float x) { return (XGB_ORACLE_CR & 8) ? (float)expl((long double)x) : std::exp(x); }
+inline float crLog(float x) { return (XGB_ORACLE_CR & 16) ? (float)logl((long double)x) : std::log(x); }
+inline float crAsin(float x) { return (XGB_ORACLE_CR & 32) ? (float)asinl((long double)x) : std::asin(x); }
+inline float crAcos(float x) { return (XGB_ORACLE_CR & 64) ? (float)acosl((long double)x) : std::acos(x); }
+inline float crAtan2(float y, float x) {
+    return (XGB_ORACLE_CR & 128) ? (float)atan2l((long double)y, (long double)x) : std::atan2(y, x);
+}
+#define sinf crSin
+#define cosf crCos
+#define powf crPow
+#define expf crExp
+#define logf crLog
+#define asinf crAsin
+#define acosf crAcos
+#define atan2f crAtan2
+#endif
+
 const float kPi = (float)M_PI;  // Utils.h:32
 const float kInf = std::numeric_limits<float>::infinity();
 
@@ -1370,10 +1399,17 @@ Ray cameraRay(const Scene& sc, float fx, float fy) {
 
 }  // namespace
 
-#ifdef XGB_ORACLE_ULP_PERTURB
+#if defined(XGB_ORACLE_ULP_PERTURB) || defined(XGB_ORACLE_CR)
 #undef cosf
 #undef sinf
 #undef powf
+#undef expf
+#undef logf
+#undef asinf
+#endif
+#ifdef XGB_ORACLE_CR
+#undef acosf
+#undef atan2f
 #endif
 
 // ------------------------------------------------------------------ C API --

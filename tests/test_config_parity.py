@@ -18,7 +18,13 @@ workload the benchmark measures is checked at the size it is measured on:
 
 Tolerance (floating point, the bar of the whole path): relMSE <= 1e-4 with
 eps = 1e-2 and at least 98 % of pixel channels within 1e-3 relative; no device
-error bit. The oracle runs on all host cores.
+error bit. The oracle runs on all host cores. The room's paths (14 diffuse
+segments on average among 200k interpenetrating boxes) are long enough that the
+C library's own misrounded sinf / cosf (about 1 % of the azimuths the
+diffuse sampler draws) send a few paths elsewhere: the oracle built with
+correctly rounded functions differs from the plain oracle by relMSE ~1.3e-4
+there. The GPU must match that correctly rounded oracle to 1e-8, and the plain
+one to 1e-4 or 1.5 times that envelope, whichever is larger.
 """
 import numpy as np
 import pytest
@@ -92,7 +98,20 @@ def test_occluded_room_reference_defaults(api_ctx):
     api, ctx = api_ctx
     desc = scenes.occluded_room(128, 128, 4)
     assert desc.params.max_depth == 0 and desc.n_tris > 200_000
-    _render_and_check(api, ctx, desc)
+    b = api.load_scene(ctx, desc)
+    rt = api.RenderTarget(ctx, desc.width, desc.height)
+    rt.render(b.scene, desc.spp, desc.params)
+    gpu = rt.download()
+    assert b.scene.stats()["error_flags"] == 0
+    cpu = load_cpu(desc, "port").render_pcg(desc)
+    cr = load_cpu(desc, "port_cr255").render_pcg(desc)
+    err, err_cr, envelope = relmse(gpu, cpu), relmse(gpu, cr), relmse(cr, cpu)
+    print(f"occluded room: relMSE {err:.3e} (within 1e-3: {_close(gpu, cpu):.4f}), against the correctly "
+          f"rounded oracle {err_cr:.3e}, C-library envelope {envelope:.3e}")
+    assert np.isfinite(gpu).all()
+    assert err_cr <= 1e-8
+    assert err <= max(TOL, 1.5 * envelope)
+    assert _close(gpu, cpu) >= 0.98
 
 
 def test_batch_with_largest_jobs(api_ctx):

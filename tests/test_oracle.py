@@ -94,17 +94,21 @@ def test_reference_rejects_non_default_params():
 
 def test_mfnm_amplifies_last_ulp_differences():
     """MicrofacetNormalMapping (Sandbox/MicrofacetBasedNormalMapping/Main.cpp:86-340)
-    builds its tangent facet from sqrt(1 - dot(wp, wg)^2) with dot ~ 1 and feeds the
-    result into random-walk decisions, so a one-ulp change in cosf / sinf / powf flips
-    whole paths. The same probe leaves the Lambert/GGX scenes within 1e-4. This is the
-    envelope the GPU's MFNM parity check uses (CUDA and glibc libm differ by an ulp)."""
+    feeds sampled directions into random-walk decisions, so a one-ulp change in every
+    cosf / sinf / powf result flips whole paths. The same probe leaves the Lambert/GGX
+    scenes within 1e-4. Correct rounding is a different matter: the C library rounds
+    these functions correctly for all but ~1 % of arguments, and the oracle whose
+    functions all round correctly (what the GPU's samplers compute) stays within 1e-5
+    of the plain oracle on the same scene."""
     from xitils_gb300.scene import IntegratorParams
     P = IntegratorParams()
     mf = scenes.material_zoo(64, 64, 8, sky="none", only=[0])
     a = load_scene(mf, "port").render_pcg(mf, params=P)
     b = load_scene(mf, "port_ulp").render_pcg(mf, params=P)
+    c = load_scene(mf, "port_cr255").render_pcg(mf, params=P)
     from oracle.bindings import relmse
     assert relmse(b, a) > 1e-3
+    assert relmse(c, a) < 1e-5
     cb = scenes.cornell(64, 64, 8)
     a = load_scene(cb, "port").render_pcg(cb)
     b = load_scene(cb, "port_ulp").render_pcg(cb)

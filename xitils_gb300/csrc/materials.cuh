@@ -4,8 +4,13 @@
 // Expression order follows the reference; this header is compiled with
 // -fmad=false so float arithmetic is unfused as in the reference. Where the
 // reference promotes an intermediate to double (M_PI literals, pow(float, int)),
-// the device evaluates in float: results differ by at most a few ulp.
+// the device evaluates in float (values differ by at most a few ulp), except in
+// the arguments of sampled directions, which the reference rounds from double
+// (2 * M_PI * u): those are evaluated as the reference does. The samplers call
+// the correctly rounded functions of crmath.cuh, as the C library rounds; value
+// computations (BSDF values, densities, sky lookups) use CUDA's own functions.
 #pragma once
+#include "crmath.cuh"
 #include "xgb_math.cuh"
 #include "xgb_types.h"
 
@@ -88,10 +93,13 @@ __device__ __forceinline__ V3 vmf4SampleRef(const float4* L, Pcg& rng) {
     const float v = rng.randf();
     const float r = sqrtf(u);
     const float theta = (float)((double)(2.0f * kPi * v) - kPiD);
-    const float vx = r * cosf(theta), vy = r * sinf(theta);
+    float st, ct;
+    crSinCosf(theta, &st, &ct);
+    const float vx = r * ct, vy = r * st;
     const float u2 = rng.randf();
-    const float W = kappa > 0.0f ? 1.0f + powf(kappa, -1.0f) * logf(u2 + (1.0f - u2) * expf(-2.0f * kappa)) : 1.0f;
-    const float sq = safeSqrt(1.0f - powf(W, 2.0f));
+    const float W =
+        kappa > 0.0f ? 1.0f + crPowf(kappa, -1.0f) * crLogf(u2 + (1.0f - u2) * crExpf(-2.0f * kappa)) : 1.0f;
+    const float sq = safeSqrt(1.0f - W * W);  // powf(W, 2) rounds W^2 once, as the product does
     Basis basis(normalize(mu));
     return normalize(basis.toGlobal(W, sq * vx, sq * vy));
 }
@@ -178,9 +186,11 @@ struct MetalD {  // Material.h:275-384
         float U1 = rng.randf();
         float U2 = rng.randf();
         float r = sqrtf(U1);
-        float phi = 2.0f * kPi * U2;
-        float t1 = r * cosf(phi);
-        float t2 = r * sinf(phi);
+        float phi = (float)(2.0 * kPiD * (double)U2);  // 2.0f * M_PI * U2 in double, as the reference
+        float sp, cp;
+        crSinCosf(phi, &sp, &cp);
+        float t1 = r * cp;
+        float t2 = r * sp;
         float s = 0.5f * (1.0f + Vh.x);
         t2 = (1.0f - s) * sqrtf(1.0f - t1 * t1) + s * t2;
         V3 Nh = t1 * T1 + t2 * T2 + safeSqrt(1.0f - t1 * t1 - t2 * t2) * Vh;
@@ -233,9 +243,10 @@ struct GlossyD {  // Material.h:88-132; clamped: Main.cpp:34-84
         float r1 = rng.randf();
         float r2 = rng.randf();
         Basis basis(s.sn);
-        float sq = safeSqrt(1 - powf(r2, 2 / (sh + 1.0f)));
-        float ph = 2 * kPi * r1;
-        V3 h = normalize(basis.toGlobal(powf(r2, 1 / (sh + 1.0f)), cosf(ph) * sq, sinf(ph) * sq));
+        float sq = safeSqrt(1 - crPowf(r2, 2 / (sh + 1.0f)));
+        float sp, cp;
+        crSinCosf((float)(2.0 * kPiD * (double)r1), &sp, &cp);  // cosf(2 * M_PI * r1): the argument in double
+        V3 h = normalize(basis.toGlobal(crPowf(r2, 1 / (sh + 1.0f)), cp * sq, sp * sq));
         *wi = -normalize(s.wo - (2.0f * dot(s.wo, h)) * h);
         *p = pdf(s, *wi);
         if (*p == 0.0f) return V3(0.0f);
@@ -304,7 +315,9 @@ __device__ __forceinline__ V3 sampleBasic(const SceneDev& sc, const Material& m,
         float u = rng.randf() * 1.0f;
         float r = sqrtf(u);
         float phi = rng.randf() * (2.0f * kPi);
-        *wi = basis.toGlobal(safeSqrt(1.0f - u), r * cosf(phi), r * sinf(phi));
+        float sp, cp;
+        crSinCosf(phi, &sp, &cp);
+        *wi = basis.toGlobal(safeSqrt(1.0f - u), r * cp, r * sp);
         *pdf = dot(*wi, s.sn) / kPi;
         V3 a(m.albedo.x, m.albedo.y, m.albedo.z);
         if (m.tex >= 0) a = a * texLookup(sc.textures[m.tex], s.uv.x, s.uv.y);

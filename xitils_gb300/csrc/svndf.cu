@@ -11,8 +11,10 @@
 // -fmad=false): the block's normals in row-major order, the mean height as a
 // sequential sum, the E-step over samples (responsibilities without the lobe
 // weights, as the reference computes them), the M-step sums per lobe in sample
-// order, the signed convergence difference. Only CUDA's expf / powf / asinf / cosf
-// / sinf differ from the C library's by an ulp or so.
+// order, the signed convergence difference. The EM stops on a threshold, so the
+// fit is chaotic at the last ulp: exp, pow, asin, sin and cos are the correctly
+// rounded ones of crmath.cuh, which round as the C library does for all but a
+// small fraction of arguments.
 #include <algorithm>
 
 #include "xgb_kernels.h"
@@ -40,7 +42,7 @@ struct SvWarp {
 // vMF() (VonMisesFisherDistribution.h:205-211)
 __device__ __forceinline__ float vmfLobe(V3 mu, float kappa, V3 omega) {
     if (kappa == 0.0f) return 1.0f / (4 * kPi);
-    return kappa / (2 * kPi * (1.0f - expf(-2 * kappa))) * expf(kappa * (dot(omega, mu) - 1.0f));
+    return kappa / (2 * kPi * (1.0f - crExpf(-2 * kappa))) * crExpf(kappa * (dot(omega, mu) - 1.0f));
 }
 
 __global__ void __launch_bounds__(32 * kSvWarps) k_svndfFit(TextureDev src, float scale, int rate, uint32_t seed,
@@ -80,11 +82,14 @@ __global__ void __launch_bounds__(32 * kSvWarps) k_svndfFit(TextureDev src, floa
         for (int j = 0; j < kSvndfLobes; ++j) {
             const float u = rng.randf();
             const float v = rng.randf();
-            const float theta = asinf(u);
+            const float theta = crAsinf(u);
             const float phi = (float)((double)(2.0f * kPi * v) - kPiD);
-            S.mu[j][0] = cosf(theta) * cosf(phi);
-            S.mu[j][1] = cosf(theta) * sinf(phi);
-            S.mu[j][2] = sinf(theta);
+            float st, ct, sp, cp;
+            crSinCosf(theta, &st, &ct);
+            crSinCosf(phi, &sp, &cp);
+            S.mu[j][0] = ct * cp;
+            S.mu[j][1] = ct * sp;
+            S.mu[j][2] = st;
             S.kappa[j] = 0.5f;
             S.alpha[j] = 1.0f / kSvndfLobes;
         }
@@ -119,7 +124,7 @@ __global__ void __launch_bounds__(32 * kSvWarps) k_svndfFit(TextureDev src, floa
             r = r / a;
             a /= (float)n;
             const float len = length(r);
-            float kappa = (3 * len - powf(len, 3.0f)) / (1.0f - dot(r, r));
+            float kappa = (3 * len - crPowf(len, 3.0f)) / (1.0f - dot(r, r));
             const V3 mu = normalize(r);
             if (kappa > kSvKappaLimit) kappa = kSvKappaLimit;
             if (kappa < 0.0f) kappa = 0.0f;
