@@ -73,7 +73,8 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="xgb", choices=["xgb", "reference"])
-    p.add_argument("--workload", default="terrain", choices=["terrain", "cornell", "shell", "svbrdf", "batch", "mfnm"])
+    p.add_argument("--workload", default="terrain",
+                   choices=["terrain", "cornell", "room", "shell", "svbrdf", "batch", "mfnm"])
     p.add_argument("--shell-grid", type=int, default=256)
     p.add_argument("--mfnm-res", type=int, default=2048)
     p.add_argument("--mfnm-ref-spp", type=int, default=2048)
@@ -127,6 +128,14 @@ def make_workload(args):
         meta = {"data": "synthetic (seeded cloth patch, procedural plain-weave displacement map)",
                 "kernel": "k_trace_flat2 (closest-hit traversal of <= 16 instances with the shell-mapping discard, persistent)",
                 "l2": big}
+    elif args.workload == "room":
+        res = args.res or 1024
+        spp = args.spp or 4
+        desc = scenes.occluded_room(res, res, spp)
+        label = (f"occluded room ({desc.n_tris} tris: 16,667 random boxes in a 10x4x10 room, light behind a slit), "
+                 f"{res}x{res} film, {spp} spp, reference defaults (no depth limit, RR after 5 at 0.9)")
+        meta = {"data": "synthetic (seeded random boxes)", "kernel": FLAT_KERNEL,
+                "l2": "the scene (BVH + triangles, about 23 MB) fits in L2; path queues of 2^23 paths stream through HBM"}
     else:
         res = args.res or 512
         spp = args.spp or 16

@@ -56,6 +56,13 @@ xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder);
 #define XGB_BVH_BINARY 0
 #define XGB_BVH_WIDE8 1
 xgb_status xgb_ctx_set_bvh_layout(xgb_ctx* ctx, int layout);
+/* Order in which xgb_render fills its wavefront with camera paths: pixel blocks
+ * of tile_w x tile_h (rows in bands of tile_h, a band block by block), so that
+ * neighbouring paths start close together; 0, 0 = scanline rows (default). The
+ * per-pixel random streams make the image independent of the order: this
+ * changes speed only. The reference renders 16 x 16 tiles on OpenMP threads
+ * (Include/Xitils/RenderTarget.h:58-59, :110-113). */
+xgb_status xgb_ctx_set_path_order(xgb_ctx* ctx, int tile_w, int tile_h);
 /* Waits for the work enqueued on stream (NULL = the context's own stream). */
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream);
 /* Last error message of this context ("" when none). Never NULL. */

@@ -180,3 +180,28 @@ def test_mfnm_at_scale_small(ctx):
     assert close >= 0.98
     err_cr, _ = _against_cr_oracle(gpu, desc, desc.params)
     assert err_cr <= CR_TOL
+
+
+def test_tiled_path_order_same_image(ctx):
+    """Camera paths in pixel blocks instead of scanline rows (xgb_ctx_set_path_order):
+    every pixel keeps its own per-sample random streams, so the film equals the
+    scanline film up to the order of the FP32 additions (bijective pixel mapping),
+    for block sides that divide the film and ones that leave ragged edges."""
+    from xitils_gb300 import api
+    desc = scenes.cornell(50, 37, 4)
+    b = api.load_scene(ctx, desc)
+    base = api.RenderTarget(ctx, desc.width, desc.height)
+    base.render(b.scene, desc.spp, desc.params)
+    want = base.download()
+    try:
+        for tw, th in ((8, 4), (4, 8), (7, 3), (64, 64), (1, 1)):
+            ctx.set_path_order(tw, th)
+            rt = api.RenderTarget(ctx, desc.width, desc.height)
+            rt.render(b.scene, desc.spp, desc.params)
+            np.testing.assert_allclose(rt.download(), want, rtol=1e-5, atol=1e-6, err_msg=f"tile {tw}x{th}")
+            assert b.scene.stats()["paths"] == desc.n_paths
+    finally:
+        ctx.set_path_order(0, 0)
+    for tw, th in ((0, 4), (-1, -1), (257, 1)):
+        with pytest.raises(api.XgbError):
+            ctx.set_path_order(tw, th)

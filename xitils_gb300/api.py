@@ -73,6 +73,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_ctx_synchronize": [P, P],
         "xgb_ctx_set_bvh_builder": [P, C.c_int],
         "xgb_ctx_set_bvh_layout": [P, C.c_int],
+        "xgb_ctx_set_path_order": [P, C.c_int, C.c_int],
         "xgb_scene_intersect": [P, C.c_int, FP, FP, P],
         "xgb_scene_occluded": [P, C.c_int, FP, C.POINTER(C.c_int32), P],
         "xgb_film_enable_aovs": [P],
@@ -195,6 +196,10 @@ class Context:
     def set_bvh_layout(self, name: str):
         """Node layout of the BVH of meshes created afterwards: "binary" (default) or "wide8"."""
         self.check(self.lib.xgb_ctx_set_bvh_layout(self.h, self.BVH_LAYOUTS[name]), "set_bvh_layout")
+
+    def set_path_order(self, tile_w: int = 0, tile_h: int = 0):
+        """Camera paths in tile_w x tile_h pixel blocks (0, 0 = scanline rows); speed only."""
+        self.check(self.lib.xgb_ctx_set_path_order(self.h, int(tile_w), int(tile_h)), "set_path_order")
 
     def synchronize(self, stream=None):
         self.check(self.lib.xgb_ctx_synchronize(self.h, stream), "synchronize")

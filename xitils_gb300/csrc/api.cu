@@ -94,6 +94,7 @@ struct xgb_ctx {
     std::string err;
     int bvhBuilder = kBuilderPloc;
     int bvhLayout = kLayoutBinary;
+    int tileW = 0, tileH = 0;  // camera-path order (xgb_ctx_set_path_order)
 };
 
 struct xgb_texture {
@@ -271,6 +272,15 @@ xgb_status xgb_ctx_set_bvh_builder(xgb_ctx* ctx, int builder) {
     if (builder != XGB_BVH_PLOC && builder != XGB_BVH_LBVH)
         return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_bvh_builder: unknown builder");
     ctx->bvhBuilder = builder == XGB_BVH_PLOC ? kBuilderPloc : kBuilderLbvh;
+    return XGB_OK;
+}
+
+xgb_status xgb_ctx_set_path_order(xgb_ctx* ctx, int tile_w, int tile_h) {
+    if (!ctx) return XGB_INVALID_ARG;
+    if (tile_w < 0 || tile_h < 0 || tile_w > 256 || tile_h > 256 || (tile_w == 0) != (tile_h == 0))
+        return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_path_order: tile sides in [1, 256], or both 0");
+    ctx->tileW = tile_w;
+    ctx->tileH = tile_h;
     return XGB_OK;
 }
 
@@ -1245,6 +1255,8 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.film = film->d;
     rp.aov = film->aov;
     rp.dropNonFinite = (s->fixes & XGB_FIX_DROP_NONFINITE) ? 1 : 0;
+    rp.tileW = ctx->tileW;
+    rp.tileH = ctx->tileH;
     rp.guided = 0;
     rp.train = 0;
     rp.bsdfFrac = s->bsdfFrac;

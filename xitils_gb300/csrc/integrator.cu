@@ -34,6 +34,34 @@ __global__ void k_plan(Ctrl* c, unsigned int capacity) {
 
 // Camera paths: RenderTargetTile::GenerateFilmPosition (RenderTarget.h:68-80)
 // then PinholeCamera::generateRay (Camera.h:45-55).
+// Pixel of the i-th camera path of a sample pass when paths are ordered in
+// tw x th pixel blocks: rows in bands of th, a band's pixels block by block
+// (row-major inside a block, the last block of a band as wide as what is left),
+// so that a warp's 32 paths start from a compact patch of the film. Bijective on
+// [0, W H) for any W, H; the per-pixel random streams make the image
+// independent of the order.
+__device__ __forceinline__ unsigned int tiledPixel(unsigned int i, unsigned int W, unsigned int H, unsigned int tw,
+                                                   unsigned int th) {
+    const unsigned int band = i / (W * th);
+    const unsigned int y0 = band * th;
+    const unsigned int hb = min(th, H - y0);
+    const unsigned int j = i - band * W * th;
+    const unsigned int blockSize = tw * hb;
+    const unsigned int full = W / tw;
+    unsigned int x, y;
+    if (j < full * blockSize) {
+        const unsigned int b = j / blockSize, k = j - b * blockSize;
+        x = b * tw + k % tw;
+        y = y0 + k / tw;
+    } else {
+        const unsigned int rem = W - full * tw;
+        const unsigned int k = j - full * blockSize;
+        x = full * tw + k % rem;
+        y = y0 + k / rem;
+    }
+    return x + y * W;
+}
+
 template <class J>
 __global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, const Ctrl* ctrl) {
     const unsigned int nCont = ctrl->nCont, nActive = ctrl->nActive;
@@ -47,6 +75,8 @@ __global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, c
         const unsigned int px = (unsigned int)rp.width * (unsigned int)rp.height;
         unsigned int sample = rp.sppBegin + (unsigned int)(local / px);
         unsigned int pix = (unsigned int)(local % px);
+        if (rp.tileW > 0) pix = tiledPixel(pix, (unsigned int)rp.width, (unsigned int)rp.height, (unsigned int)rp.tileW,
+                                           (unsigned int)rp.tileH);
         int x = (int)(pix % (unsigned int)rp.width), y = (int)(pix / (unsigned int)rp.width);
         Pcg rng;
         rng.seed(pix, sample, rp.seed);

@@ -130,6 +130,9 @@ struct RenderParams {
     int arenaCap;
     float recordProb;         // probability that a guided vertex becomes a record
     float4* pathAcc;          // per path of the call: contributions so far (rgb)
+    // order of the camera paths of a sample pass: tileW x tileH pixel blocks
+    // (k_generate), 0 = scanline rows
+    int tileW, tileH;
 };
 
 // Device arrays of a batch of render jobs sharing one wavefront (xgb_render_batch):
