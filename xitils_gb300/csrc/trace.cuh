@@ -151,12 +151,17 @@ __device__ __forceinline__ void wideHeader(const WNode* nd, WideHdr& h) {
 
 // Tests the eight child boxes of a node; returns the hit children as bits at
 // position slot ^ oct (lowest bit first = roughly nearest first).
-// Per axis the plane distance is t = q * (2^e / d) + (p - o) / d, one FMA per
-// plane, with the byte q turned into a float exactly (0x4B0000qq - 2^23). The
-// near plane of each axis is the low one for a positive direction component
-// and the high one for a negative one. The quantised boxes already reach one
-// quantisation step beyond the child's true box, which covers the rounding of
-// this form; the far distance is widened by 2^-20 relative as in slab().
+// Per axis the plane distance is t = q * (2^e / d) + (p - o) / d. The byte q is
+// turned into the float Q = 2^23 + q by a byte permute (0x4B0000qq), and the
+// 2^23 is folded into the per-node offset, b' = (p - o) / d - 2^23 (2^e / d), so
+// that each plane costs one permute and one FMA: t = Q (2^e / d) + b'. Rounding
+// b' moves a plane by at most half a quantisation step (or an ulp of the offset
+// when that is larger); the quantised boxes reach at least one step beyond the
+// child's true box and the far distance is widened by 2^-20 relative as in
+// slab(), so the test stays conservative. The near plane of each axis is the
+// low one for a positive direction component and the high one for a negative
+// one. Empty slots hold inverted boxes (low 255, high 0), which no ray accepts,
+// so every slot is tested without a branch.
 __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r, int oct, float tMax, WideHdr& h) {
     const float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c), d = __ldg(&nd->d), e = __ldg(&nd->e);
     const unsigned int bits = __float_as_uint(a.w);
@@ -168,7 +173,9 @@ __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r,
     const float scx = __uint_as_float((bits & 0xFFu) << 23) * r.ix;
     const float scy = __uint_as_float(((bits >> 8) & 0xFFu) << 23) * r.iy;
     const float scz = __uint_as_float(((bits >> 16) & 0xFFu) << 23) * r.iz;
-    const float bx = (a.x - r.ox) * r.ix, by = (a.y - r.oy) * r.iy, bz = (a.z - r.oz) * r.iz;
+    const float bx = fmaf(-8388608.0f, scx, (a.x - r.ox) * r.ix);
+    const float by = fmaf(-8388608.0f, scy, (a.y - r.oy) * r.iy);
+    const float bz = fmaf(-8388608.0f, scz, (a.z - r.oz) * r.iz);
     const unsigned int lx0 = __float_as_uint(c.x), lx1 = __float_as_uint(c.y);
     const unsigned int ly0 = __float_as_uint(c.z), ly1 = __float_as_uint(c.w);
     const unsigned int lz0 = __float_as_uint(d.x), lz1 = __float_as_uint(d.y);
@@ -179,21 +186,20 @@ __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r,
     const unsigned int nx[2] = {fx ? hx0 : lx0, fx ? hx1 : lx1}, xx[2] = {fx ? lx0 : hx0, fx ? lx1 : hx1};
     const unsigned int ny[2] = {fy ? hy0 : ly0, fy ? hy1 : ly1}, xy[2] = {fy ? ly0 : hy0, fy ? ly1 : hy1};
     const unsigned int nz[2] = {fz ? hz0 : lz0, fz ? hz1 : lz1}, xz[2] = {fz ? lz0 : hz0, fz ? lz1 : hz1};
+    const float tLim = tMax;
     unsigned int mask = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int w = s >> 2;
         const unsigned int sel = 0x7540u | (unsigned int)(s & 3);
-        const unsigned int mb = byteOf(w ? h.meta1 : h.meta0, s);
-        if (!((h.imask >> s) & 1u) && mb == 0u) continue;  // empty slot
-        const float qnx = __uint_as_float(__byte_perm(nx[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float qny = __uint_as_float(__byte_perm(ny[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float qnz = __uint_as_float(__byte_perm(nz[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float qfx = __uint_as_float(__byte_perm(xx[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float qfy = __uint_as_float(__byte_perm(xy[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float qfz = __uint_as_float(__byte_perm(xz[w], 0x4B000000u, sel)) - 8388608.0f;
-        const float tn = fmaxf(fmaxf(fmaf(qnx, scx, bx), fmaf(qny, scy, by)), fmaxf(fmaf(qnz, scz, bz), 0.0f));
-        const float tf = fminf(fminf(fmaf(qfx, scx, bx), fmaf(qfy, scy, by)), fminf(fmaf(qfz, scz, bz), tMax));
+        const float tnx = fmaf(__uint_as_float(__byte_perm(nx[w], 0x4B000000u, sel)), scx, bx);
+        const float tny = fmaf(__uint_as_float(__byte_perm(ny[w], 0x4B000000u, sel)), scy, by);
+        const float tnz = fmaf(__uint_as_float(__byte_perm(nz[w], 0x4B000000u, sel)), scz, bz);
+        const float tfx = fmaf(__uint_as_float(__byte_perm(xx[w], 0x4B000000u, sel)), scx, bx);
+        const float tfy = fmaf(__uint_as_float(__byte_perm(xy[w], 0x4B000000u, sel)), scy, by);
+        const float tfz = fmaf(__uint_as_float(__byte_perm(xz[w], 0x4B000000u, sel)), scz, bz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tLim));
         if (tn <= tf * 1.00000095367431640625f) mask |= 1u << (s ^ oct);
     }
     return mask;
