@@ -21,10 +21,12 @@ Guided section (rank 0, after the throughput measurement; --no-guided skips it):
   path on the occluded-light room (10 x 4 x 10 room, 16,667 seeded boxes =
   200,026 triangles, 0.5 x 0.5 light of radiance 200 behind a wall with a
   1.0 x 0.2 gap; reference defaults: no depth limit, Russian roulette after 5 at
-  0.9), --guided-res square film, --guided-seconds per arm, training during the
-  first 25 % of the guided arm's time (Adam, lr 1e-3, one-sample MIS with BSDF
-  fraction 0.5), against a --guided-ref-spp plain reference rendered as two
-  halves (FP64 films) whose own relMSE estimate is reported beside the ratio.
+  0.9), --guided-res square film (default 1024 x 1024, the configuration's),
+  --guided-seconds per arm, training during the first 25 % of the guided arm's
+  time (Adam, lr 1e-3, one-sample MIS with BSDF fraction 0.5), against a
+  --guided-ref-spp plain reference rendered as two halves (FP64 films) whose own
+  relMSE estimate is reported beside the ratio; also MSE, a breakdown of both
+  over the reference's luminance and the network's share of guided render time.
 
 Multi-GPU (torchrun, N > 1): replicas -- every rank renders its own disjoint
 sample range of the same film (weak scaling, no data-path collective); the
@@ -88,9 +90,9 @@ def parse():
     p.add_argument("--no-guided", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the Cornell, small-batch and reference-defaults measurements after the main line")
-    p.add_argument("--guided-res", type=int, default=512)
-    p.add_argument("--guided-seconds", type=float, default=8.0)
-    p.add_argument("--guided-ref-spp", type=int, default=16384)
+    p.add_argument("--guided-res", type=int, default=1024)
+    p.add_argument("--guided-seconds", type=float, default=15.0)
+    p.add_argument("--guided-ref-spp", type=int, default=4096)
     p.add_argument("--guided-pass-spp", type=int, default=16)
     p.add_argument("--guided-train-pass-spp", type=int, default=4)
     p.add_argument("--guided-max-steps", type=int, default=512)

@@ -286,6 +286,11 @@ typedef struct {
     double kernel_ms[5];
     uint64_t stage_launches[5];
     uint64_t guide_train_steps; /* Adam steps of the learned proposal taken by the call */
+    /* profiled calls with a learned proposal: device time of its per-path network
+       inference (not part of kernel_ms) and of the end-of-call training (record
+       finalisation, pooling, Adam steps) */
+    double guide_infer_ms;
+    double guide_train_ms;
 } xgb_render_stats;
 
 /* ------------------------------------------------------- batched renders */

@@ -51,7 +51,7 @@ class RenderStatsC(C.Structure):
                 ("iterations", C.c_uint64), ("kernel_launches", C.c_uint64), ("node_visits", C.c_uint64),
                 ("tri_tests", C.c_uint64), ("error_flags", C.c_uint32), ("profiled", C.c_uint32),
                 ("kernel_ms", C.c_double * 5), ("stage_launches", C.c_uint64 * 5),
-                ("guide_train_steps", C.c_uint64)]
+                ("guide_train_steps", C.c_uint64), ("guide_infer_ms", C.c_double), ("guide_train_ms", C.c_double)]
 
 
 _lib = None
@@ -495,7 +495,10 @@ class Scene:
         out = {}
         for k, _ in RenderStatsC._fields_:
             v = getattr(s, k)
-            out[k] = list(v) if k in ("kernel_ms", "stage_launches") else int(v)
+            if k in ("kernel_ms", "stage_launches"):
+                out[k] = list(v)
+            else:
+                out[k] = float(v) if k.endswith("_ms") else int(v)
         return out
 
 
@@ -595,8 +598,11 @@ def batch_autotune(ctx: Context, jobs, stream=None) -> dict:
 def batch_stats(ctx: Context) -> dict:
     s = RenderStatsC()
     ctx.check(ctx.lib.xgb_batch_stats_get(ctx.h, C.byref(s)), "batch_stats")
-    return {k: (list(getattr(s, k)) if k in ("kernel_ms", "stage_launches") else int(getattr(s, k)))
-            for k, _ in RenderStatsC._fields_}
+    out = {}
+    for k, _ in RenderStatsC._fields_:
+        v = getattr(s, k)
+        out[k] = list(v) if k in ("kernel_ms", "stage_launches") else (float(v) if k.endswith("_ms") else int(v))
+    return out
 
 
 def write_png(path: str, rgb: np.ndarray) -> None:

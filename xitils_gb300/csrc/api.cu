@@ -1316,35 +1316,38 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     int parity = 0;
     const int kIterPerCheck = 8;
     const bool prof = s->profiling;
-    if (prof && s->events.size() < 6 * kIterPerCheck) {
-        while (s->events.size() < 6 * kIterPerCheck) {
+    constexpr int kEv = 7;  // per iteration: plan, generate, extend, guide inference, shade, shadow, end
+    if (prof && s->events.size() < kEv * kIterPerCheck + 2) {
+        while (s->events.size() < kEv * kIterPerCheck + 2) {
             cudaEvent_t ev;
             XGB_CUDA(ctx, cudaEventCreate(&ev));
             s->events.push_back(ev);
         }
     }
     double stageMs[5] = {0, 0, 0, 0, 0};
+    double inferMs = 0.0, trainMs = 0.0;
     uint64_t launches = 0;
     for (int guard = 0;; ++guard) {
         for (int k = 0; k < kIterPerCheck; ++k) {
             PathQueue& X = s->rb.q[parity];
             PathQueue& Y = s->rb.q[parity ^ 1];
-            cudaEvent_t* ev = prof ? &s->events[6 * k] : nullptr;
+            cudaEvent_t* ev = prof ? &s->events[kEv * k] : nullptr;
             if (prof) cudaEventRecord(ev[0], st);
             launchPlan(s->ctrl, cap, st);
             if (prof) cudaEventRecord(ev[1], st);
             launchGenerate(s->sd, rp, X, s->ctrl, gShade, st);
             if (prof) cudaEventRecord(ev[2], st);
             launchExtend(s->sd, X, s->rb.hits, s->ctrl, ctx->numSMs, prof, st);
+            if (prof) cudaEventRecord(ev[3], st);
             if (gd) {
                 guideInferPaths(s->sd, gd->g, gb, X, s->rb.hits, s->ctrl, s->mix, gShade, st);
                 ++launches;
             }
-            if (prof) cudaEventRecord(ev[3], st);
-            launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, ctx->numSMs, st);
             if (prof) cudaEventRecord(ev[4], st);
-            launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, ctx->numSMs, st);
+            launchShade(s->sd, rp, X, s->rb.hits, Y, s->rb.shadow, s->ctrl, ctx->numSMs, st);
             if (prof) cudaEventRecord(ev[5], st);
+            launchShadow(s->sd, rp, s->rb.shadow, Y, s->ctrl, ctx->numSMs, st);
+            if (prof) cudaEventRecord(ev[6], st);
             launches += 5;
             parity ^= 1;
         }
@@ -1352,18 +1355,25 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
         XGB_CUDA(ctx, cudaMemcpyAsync(s->ctrlHost, s->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st));
         XGB_CUDA(ctx, cudaStreamSynchronize(st));
         if (prof) {
-            for (int k = 0; k < kIterPerCheck; ++k)
-                for (int j = 0; j < 5; ++j) {
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, s->events[6 * k + j], s->events[6 * k + j + 1]);
-                    stageMs[j] += ms;
-                }
+            // stages: plan, generate, extend, [guide inference], shade, shadow
+            for (int k = 0; k < kIterPerCheck; ++k) {
+                float ms[6] = {0, 0, 0, 0, 0, 0};
+                for (int j = 0; j < 6; ++j)
+                    cudaEventElapsedTime(&ms[j], s->events[kEv * k + j], s->events[kEv * k + j + 1]);
+                stageMs[0] += ms[0];
+                stageMs[1] += ms[1];
+                stageMs[2] += ms[2];
+                inferMs += ms[3];
+                stageMs[3] += ms[4];
+                stageMs[4] += ms[5];
+            }
         }
         const Ctrl& c = *s->ctrlHost;
         if (c.nextPath >= c.totalPaths && c.nOut == 0) break;
         if (guard > (1 << 22)) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: wavefront did not drain");
     }
     if (gd && rp.train) {
+        if (prof) cudaEventRecord(s->events[kEv * kIterPerCheck], st);
         // every path of the call has finished: records take their incident
         // radiance, those that carry some join the pool, and the pool is
         // consumed in fixed-size Adam steps
@@ -1375,6 +1385,13 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
         guideSteps += (uint64_t)n;
         launches += 2 + 2 * (uint64_t)n + 1;  // finalize, collect; two per Adam step; pool count
         XGB_CUDA(ctx, cudaGetLastError());
+        if (prof) {
+            float ms = 0.0f;
+            cudaEventRecord(s->events[kEv * kIterPerCheck + 1], st);
+            XGB_CUDA(ctx, cudaEventSynchronize(s->events[kEv * kIterPerCheck + 1]));
+            cudaEventElapsedTime(&ms, s->events[kEv * kIterPerCheck], s->events[kEv * kIterPerCheck + 1]);
+            trainMs = ms;
+        }
     }
     const Ctrl& c = *s->ctrlHost;
     if (c.pathsDone > 0) s->vertsPerPath = (double)c.extensionRays / (double)c.pathsDone;
@@ -1387,6 +1404,8 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     s->last.node_visits = c.nodeVisits;
     s->last.tri_tests = c.triTests;
     s->last.guide_train_steps = guideSteps;
+    s->last.guide_infer_ms = inferMs;
+    s->last.guide_train_ms = trainMs;
     s->last.profiled = prof ? 1 : 0;
     for (int j = 0; j < 5; ++j) {
         s->last.kernel_ms[j] = stageMs[j];

@@ -70,6 +70,52 @@ __device__ __forceinline__ void warpLayer(const __nv_bfloat16* in, int ldi, cons
     }
 }
 
+// warpLayer for 32 rows (two m16 tiles sharing every weight fragment): each
+// weight pair is loaded once per 32 rows instead of once per 16.
+template <int N, bool RELU, bool OUT_F32>
+__device__ __forceinline__ void warpLayer32(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* W, const float* bias,
+                                            __nv_bfloat16* outb, int ldo, float* outf, int ldf) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    uint32_t a[2][4][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            const __nv_bfloat16* r0 = in + (16 * m + g) * ldi + ks * 16 + 2 * t;
+            const __nv_bfloat16* r1 = r0 + 8 * ldi;
+            a[m][ks][0] = ld32(r0);
+            a[m][ks][1] = ld32(r1);
+            a[m][ks][2] = ld32(r0 + 8);
+            a[m][ks][3] = ld32(r1 + 8);
+        }
+#pragma unroll
+    for (int nt = 0; nt < N / 8; ++nt) {
+        float c[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+        const __nv_bfloat16* wr = W + (nt * 8 + g) * 64;
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            const uint32_t b0 = ld32(wr + ks * 16 + 2 * t), b1 = ld32(wr + ks * 16 + 2 * t + 8);
+            mma16816(c[0], a[0][ks], b0, b1);
+            mma16816(c[1], a[1][ks], b0, b1);
+        }
+        const int col = nt * 8 + 2 * t;
+        const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            float v0 = c[m][0] + b0, v1 = c[m][1] + b1, v2 = c[m][2] + b0, v3 = c[m][3] + b1;
+            if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f); }
+            const int r0 = 16 * m + g, r1 = r0 + 8;
+            if (OUT_F32) {
+                outf[r0 * ldf + col] = v0; outf[r0 * ldf + col + 1] = v1;
+                outf[r1 * ldf + col] = v2; outf[r1 * ldf + col + 1] = v3;
+            } else {
+                *reinterpret_cast<uint32_t*>(outb + r0 * ldo + col) = pack2(v0, v1);
+                *reinterpret_cast<uint32_t*>(outb + r1 * ldo + col) = pack2(v2, v3);
+            }
+        }
+    }
+}
+
 // --------------------------------------------------------------- training --
 // One Adam step is two launches.
 //   k_trainTiles: a CTA takes 64-row tiles of the batch (4 warps x 16 rows) and
@@ -248,10 +294,12 @@ __global__ void __launch_bounds__(128) k_trainTiles(const GuideRecord* rec, int 
                 const float p[3] = {(gd.p.x - gb.lo[0]) * gb.invExtent[0], (gd.p.y - gb.lo[1]) * gb.invExtent[1],
                                     (gd.p.z - gb.lo[2]) * gb.invExtent[2]};
                 const float nn[3] = {gd.n.x, gd.n.y, gd.n.z}, wo[3] = {gd.wo.x, gd.wo.y, gd.wo.z};
-#pragma unroll 4
+                float f[64];
+                guideFeatures(p, nn, wo, f);
+#pragma unroll
                 for (int i = 0; i < 32; i += 2)
                     *reinterpret_cast<uint32_t*>(x + i) =
-                        pack2(guideFeature(half * 32 + i, p, nn, wo), guideFeature(half * 32 + i + 1, p, nn, wo));
+                        half ? pack2(f[32 + i], f[33 + i]) : pack2(f[i], f[i + 1]);
                 if (half == 0) {
                     const float wgt = gd.pdf > 0.f ? gd.radiance / gd.pdf : 0.f;
                     S.dirw[r] = make_float4(gd.wi.x, gd.wi.y, gd.wi.z, isfinite(wgt) ? wgt : 0.f);
@@ -528,61 +576,66 @@ __global__ void k_pointFeatures(const float* p, const float* n, const float* wo,
     float pp[3] = {(p[3 * r] - gb.lo[0]) * gb.invExtent[0], (p[3 * r + 1] - gb.lo[1]) * gb.invExtent[1],
                    (p[3 * r + 2] - gb.lo[2]) * gb.invExtent[2]};
     float nn[3] = {n[3 * r], n[3 * r + 1], n[3 * r + 2]}, ww[3] = {wo[3 * r], wo[3 * r + 1], wo[3 * r + 2]};
-    for (int i = 0; i < 64; i += 2)
-        *reinterpret_cast<uint32_t*>(x + i) = pack2(guideFeature(i, pp, nn, ww), guideFeature(i + 1, pp, nn, ww));
+    float f[64];
+    guideFeatures(pp, nn, ww, f);
+#pragma unroll
+    for (int i = 0; i < 64; i += 2) *reinterpret_cast<uint32_t*>(x + i) = pack2(f[i], f[i + 1]);
 }
 
 // Per-path inference: every hit of the input queue gets its 8-lobe mixture
-// (10 float4: lobes' (mu, kappa) then the 8 weights). Warps take 16 paths; the
-// two half-warps build the two halves of each feature row.
-__global__ void __launch_bounds__(128) k_inferPaths(SceneDev sc, GuideWeights w, GuideBounds gb, PathQueue q, HitQueue h,
+// (10 float4: lobes' (mu, kappa) then the 8 weights). A warp takes 32 paths, one
+// per lane: the lane reconstructs its hit, writes its 64 features into the warp's
+// activation rows, and decodes its own output row; the four layers run as two
+// m16 tiles over the 32 rows (warpLayer32).
+__global__ void __launch_bounds__(128, 4) k_inferPaths(SceneDev sc, GuideWeights w, GuideBounds gb, PathQueue q, HitQueue h,
                                                     const Ctrl* ctrl, float4* mix) {
-    __shared__ __align__(16) __nv_bfloat16 act[4][2][16 * 72];
-    __shared__ float outY[4][16 * kGuideOutPad];
+    __shared__ __align__(16) __nv_bfloat16 act[4][2][32 * 72];
+    __shared__ float outY[4][32 * kGuideOutPad];
     const unsigned int n = ctrl->nActive;
     const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned int warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned int nWarps = (gridDim.x * blockDim.x) >> 5;
-    const int row = lane & 15, half = lane >> 4;
-    for (unsigned int base = warpGlobal * 16u; base < n; base += nWarps * 16u) {
-        const unsigned int i = base + row;
-        float pf[3] = {0.f, 0.f, 0.f}, nf[3] = {0.f, 0.f, 0.f}, wf[3] = {0.f, 0.f, 0.f};
+    for (unsigned int base = warpGlobal * 32u; base < n; base += nWarps * 32u) {
+        const unsigned int i = base + lane;
+        __nv_bfloat16* x = act[wib][0] + lane * 72;
         bool valid = false;
         if (i < n) {
-            float4 hh = h.h[i];
-            int prim = __float_as_int(hh.w);
+            const float4 hh = h.h[i];
+            const int prim = __float_as_int(hh.w);
             if (prim >= 0) {
-                float4 d4 = q.d[i];
-                Surface s = makeSurface(sc, sc.instances[h.inst[i]], prim, hh.y, hh.z, V3(d4.x, d4.y, d4.z));
-                pf[0] = (s.p.x - gb.lo[0]) * gb.invExtent[0];
-                pf[1] = (s.p.y - gb.lo[1]) * gb.invExtent[1];
-                pf[2] = (s.p.z - gb.lo[2]) * gb.invExtent[2];
-                nf[0] = s.sn.x; nf[1] = s.sn.y; nf[2] = s.sn.z;
-                wf[0] = s.wo.x; wf[1] = s.wo.y; wf[2] = s.wo.z;
+                const float4 d4 = q.d[i];
+                const Surface s = makeSurface(sc, sc.instances[h.inst[i]], prim, hh.y, hh.z, V3(d4.x, d4.y, d4.z));
+                const float pf[3] = {(s.p.x - gb.lo[0]) * gb.invExtent[0], (s.p.y - gb.lo[1]) * gb.invExtent[1],
+                                     (s.p.z - gb.lo[2]) * gb.invExtent[2]};
+                const float nf[3] = {s.sn.x, s.sn.y, s.sn.z}, wf[3] = {s.wo.x, s.wo.y, s.wo.z};
+                float f[64];
+                guideFeatures(pf, nf, wf, f);
+#pragma unroll
+                for (int k = 0; k < 64; k += 2) *reinterpret_cast<uint32_t*>(x + k) = pack2(f[k], f[k + 1]);
                 valid = true;
             }
         }
-        __nv_bfloat16* x = act[wib][0] + row * 72;
-        for (int k = half * 32; k < half * 32 + 32; k += 2)
-            *reinterpret_cast<uint32_t*>(x + k) =
-                valid ? pack2(guideFeature(k, pf, nf, wf), guideFeature(k + 1, pf, nf, wf)) : 0u;
+        if (!valid)
+#pragma unroll
+            for (int k = 0; k < 64; k += 2) *reinterpret_cast<uint32_t*>(x + k) = 0u;
         __syncwarp();
-        warpLayer<64, true, false>(act[wib][0], 72, w.W[0], w.bias[0], act[wib][1], 72, nullptr, 0);
+        warpLayer32<64, true, false>(act[wib][0], 72, w.W[0], w.bias[0], act[wib][1], 72, nullptr, 0);
         __syncwarp();
-        warpLayer<64, true, false>(act[wib][1], 72, w.W[1], w.bias[1], act[wib][0], 72, nullptr, 0);
+        warpLayer32<64, true, false>(act[wib][1], 72, w.W[1], w.bias[1], act[wib][0], 72, nullptr, 0);
         __syncwarp();
-        warpLayer<64, true, false>(act[wib][0], 72, w.W[2], w.bias[2], act[wib][1], 72, nullptr, 0);
+        warpLayer32<64, true, false>(act[wib][0], 72, w.W[2], w.bias[2], act[wib][1], 72, nullptr, 0);
         __syncwarp();
-        warpLayer<kGuideOutPad, false, true>(act[wib][1], 72, w.W[3], w.bias[3], nullptr, 0, outY[wib], kGuideOutPad);
+        warpLayer32<kGuideOutPad, false, true>(act[wib][1], 72, w.W[3], w.bias[3], nullptr, 0, outY[wib], kGuideOutPad);
         __syncwarp();
-        if (half == 0 && i < n) {
+        if (i < n) {
             VmfMixture mx;
-            decodeMixture(outY[wib] + row * kGuideOutPad, mx);
+            decodeMixture(outY[wib] + lane * kGuideOutPad, mx);
             float4* o = mix + (size_t)i * 10;
+#pragma unroll
             for (int j = 0; j < kGuideLobes; ++j)
-                o[j] = make_float4(mx.lobe[j].mu.x, mx.lobe[j].mu.y, mx.lobe[j].mu.z, mx.lobe[j].kappa);
-            o[8] = make_float4(mx.lobe[0].alpha, mx.lobe[1].alpha, mx.lobe[2].alpha, mx.lobe[3].alpha);
-            o[9] = make_float4(mx.lobe[4].alpha, mx.lobe[5].alpha, mx.lobe[6].alpha, mx.lobe[7].alpha);
+                __stcs(o + j, make_float4(mx.lobe[j].mu.x, mx.lobe[j].mu.y, mx.lobe[j].mu.z, mx.lobe[j].kappa));
+            __stcs(o + 8, make_float4(mx.lobe[0].alpha, mx.lobe[1].alpha, mx.lobe[2].alpha, mx.lobe[3].alpha));
+            __stcs(o + 9, make_float4(mx.lobe[4].alpha, mx.lobe[5].alpha, mx.lobe[6].alpha, mx.lobe[7].alpha));
         }
         __syncwarp();
     }

@@ -44,17 +44,33 @@ struct GuideBounds {
     float invExtent[3];
 };
 
-// 64 features: sin / cos of 2^b * pi * p for 6 bands and 3 axes (36), p (3), n (3), wo (3), zeros.
-__device__ __forceinline__ float guideFeature(int i, const float* p, const float* n, const float* wo) {
-    if (i < 36) {
-        int band = i / 6, rem = i % 6, axis = rem >> 1;
-        float arg = p[axis] * (float)(1 << band) * kPi;
-        return (rem & 1) ? __cosf(arg) : __sinf(arg);
+// 64 features: sin / cos of 2^b * pi * p for 6 bands and 3 axes (36), p (3), n (3), wo (3), zeros;
+// feature 6 b + 2 axis is the sine of band b, the next one its cosine. One sincos per
+// axis, the higher bands by the double-angle recurrence (sin 2a = 2 sin a cos a,
+// cos 2a = 1 - 2 sin^2 a): at band 5 it stays within 2e-5 of evaluating the band
+// directly, far inside the bf16 rounding of the network's inputs.
+__device__ __forceinline__ void guideFeatures(const float* p, const float* n, const float* wo, float* f) {
+#pragma unroll
+    for (int axis = 0; axis < 3; ++axis) {
+        float s, c;
+        __sincosf(p[axis] * kPi, &s, &c);
+#pragma unroll
+        for (int band = 0; band < kGuideBands; ++band) {
+            f[band * 6 + axis * 2] = s;
+            f[band * 6 + axis * 2 + 1] = c;
+            const float s2 = 2.0f * s * c, c2 = 1.0f - 2.0f * s * s;
+            s = s2;
+            c = c2;
+        }
     }
-    if (i < 39) return p[i - 36];
-    if (i < 42) return n[i - 39];
-    if (i < 45) return wo[i - 42];
-    return 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f[36 + k] = p[k];
+        f[39 + k] = n[k];
+        f[42 + k] = wo[k];
+    }
+#pragma unroll
+    for (int k = 45; k < 64; ++k) f[k] = 0.0f;
 }
 
 struct VmfLobe {

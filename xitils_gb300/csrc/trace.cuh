@@ -156,9 +156,9 @@ __device__ __forceinline__ void wideHeader(const WNode* nd, WideHdr& h) {
 // 2^23 is folded into the per-node offset, b' = (p - o) / d - 2^23 (2^e / d), so
 // that each plane costs one permute and one FMA: t = Q (2^e / d) + b'. Rounding
 // b' moves a plane by at most half a quantisation step (or an ulp of the offset
-// when that is larger); the quantised boxes reach at least one step beyond the
-// child's true box and the far distance is widened by 2^-20 relative as in
-// slab(), so the test stays conservative. The near plane of each axis is the
+// when that is larger); every plane is moved one more step outwards (near planes
+// by -|2^e / d|, far planes by +|2^e / d|, folded into b') and the far distance
+// is widened by 2^-20 relative as in slab(), so the test stays conservative. The near plane of each axis is the
 // low one for a positive direction component and the high one for a negative
 // one. Empty slots hold inverted boxes (low 255, high 0), which no ray accepts,
 // so every slot is tested without a branch.
@@ -176,6 +176,12 @@ __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r,
     const float bx = fmaf(-8388608.0f, scx, (a.x - r.ox) * r.ix);
     const float by = fmaf(-8388608.0f, scy, (a.y - r.oy) * r.iy);
     const float bz = fmaf(-8388608.0f, scz, (a.z - r.oz) * r.iz);
+    // one quantisation step of slack outwards on every plane (near planes earlier,
+    // far planes later): children that touch the node's own box have no padding
+    // step on that side (the byte is clamped at 0 or 255)
+    const float nbx = bx - fabsf(scx), fbx = bx + fabsf(scx);
+    const float nby = by - fabsf(scy), fby = by + fabsf(scy);
+    const float nbz = bz - fabsf(scz), fbz = bz + fabsf(scz);
     const unsigned int lx0 = __float_as_uint(c.x), lx1 = __float_as_uint(c.y);
     const unsigned int ly0 = __float_as_uint(c.z), ly1 = __float_as_uint(c.w);
     const unsigned int lz0 = __float_as_uint(d.x), lz1 = __float_as_uint(d.y);
@@ -192,12 +198,12 @@ __device__ __forceinline__ unsigned int wideEval(const WNode* nd, const WRay& r,
     for (int s = 0; s < 8; ++s) {
         const int w = s >> 2;
         const unsigned int sel = 0x7540u | (unsigned int)(s & 3);
-        const float tnx = fmaf(__uint_as_float(__byte_perm(nx[w], 0x4B000000u, sel)), scx, bx);
-        const float tny = fmaf(__uint_as_float(__byte_perm(ny[w], 0x4B000000u, sel)), scy, by);
-        const float tnz = fmaf(__uint_as_float(__byte_perm(nz[w], 0x4B000000u, sel)), scz, bz);
-        const float tfx = fmaf(__uint_as_float(__byte_perm(xx[w], 0x4B000000u, sel)), scx, bx);
-        const float tfy = fmaf(__uint_as_float(__byte_perm(xy[w], 0x4B000000u, sel)), scy, by);
-        const float tfz = fmaf(__uint_as_float(__byte_perm(xz[w], 0x4B000000u, sel)), scz, bz);
+        const float tnx = fmaf(__uint_as_float(__byte_perm(nx[w], 0x4B000000u, sel)), scx, nbx);
+        const float tny = fmaf(__uint_as_float(__byte_perm(ny[w], 0x4B000000u, sel)), scy, nby);
+        const float tnz = fmaf(__uint_as_float(__byte_perm(nz[w], 0x4B000000u, sel)), scz, nbz);
+        const float tfx = fmaf(__uint_as_float(__byte_perm(xx[w], 0x4B000000u, sel)), scx, fbx);
+        const float tfy = fmaf(__uint_as_float(__byte_perm(xy[w], 0x4B000000u, sel)), scy, fby);
+        const float tfz = fmaf(__uint_as_float(__byte_perm(xz[w], 0x4B000000u, sel)), scz, fbz);
         const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
         const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tLim));
         if (tn <= tf * 1.00000095367431640625f) mask |= 1u << (s ^ oct);

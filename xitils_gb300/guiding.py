@@ -29,6 +29,32 @@ def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
     return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
 
 
+def luminance_breakdown(plain: np.ndarray, guided: np.ndarray, ref: np.ndarray,
+                        quantiles=(0.0, 0.5, 0.9, 0.99, 1.0), eps: float = 1e-2) -> list:
+    """relMSE and MSE of both arms over pixel groups of the reference's luminance
+    (Rec. 709 weights): the dark half, the next 40 %, the next 9 % and the
+    brightest 1 % of the pixels, with each group's share of the whole image's MSE."""
+    lum = ref @ np.array([0.2126, 0.7152, 0.0722])
+    edges = np.quantile(lum, quantiles)
+    out = []
+    se_p = ((plain - ref) ** 2).mean(-1)
+    se_g = ((guided - ref) ** 2).mean(-1)
+    rel_p = ((plain - ref) ** 2 / (ref ** 2 + eps)).mean(-1)
+    rel_g = ((guided - ref) ** 2 / (ref ** 2 + eps)).mean(-1)
+    for k in range(len(quantiles) - 1):
+        lo, hi = edges[k], edges[k + 1]
+        m = (lum >= lo) & ((lum < hi) if k < len(quantiles) - 2 else (lum <= hi))
+        if not m.any():
+            continue
+        out.append({"quantiles": [quantiles[k], quantiles[k + 1]], "luminance": [float(lo), float(hi)],
+                    "pixels": int(m.sum()),
+                    "relmse_plain": float(rel_p[m].mean()), "relmse_guided": float(rel_g[m].mean()),
+                    "mse_plain": float(se_p[m].mean()), "mse_guided": float(se_g[m].mean()),
+                    "mse_share_plain": float(se_p[m].sum() / max(se_p.sum(), 1e-300)),
+                    "mse_share_guided": float(se_g[m].sum() / max(se_g.sum(), 1e-300))})
+    return out
+
+
 def render_reference(ctx: api.Context, builder: api.GpuSceneBuilder, desc: SceneDesc, spp: int,
                      chunk: int = 256, seed_offset: int = 1 << 20) -> np.ndarray:
     """Plain path tracer, FP64 film, sample indices disjoint from the compared runs."""
@@ -107,6 +133,21 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
         return train_pass_spp if state["training"] else pass_spp
 
     guided, guided_spp, guided_t = _timed_passes(ctx, builder, desc, time_s, pass_spp, params, on_pass)
+    # share of the network in a guided render: one profiled training pass and one
+    # profiled pass with the frozen network, after the timed arms
+    share = {}
+    rt = api.RenderTarget(ctx, desc.width, desc.height, fp64=True)
+    builder.scene.set_profiling(True)
+    for what, train, n in (("training_pass", True, train_pass_spp), ("frozen_pass", False, pass_spp)):
+        builder.scene.setGuide(guide, bsdf_fraction, train=train, lr=lr)
+        rt.render(builder.scene, n, params, 1 << 29)
+        st = builder.scene.stats()
+        wave = sum(st["kernel_ms"])
+        total = wave + st["guide_infer_ms"] + st["guide_train_ms"]
+        share[what] = {"spp": n, "wavefront_ms": wave, "inference_ms": st["guide_infer_ms"],
+                       "training_ms": st["guide_train_ms"], "train_steps": st["guide_train_steps"],
+                       "network_share": (st["guide_infer_ms"] + st["guide_train_ms"]) / total if total > 0 else None}
+    builder.scene.set_profiling(False)
     builder.scene.setGuide(None)
     rp, rg = relmse(plain, ref), relmse(guided, ref)
     corrected = None
@@ -122,5 +163,7 @@ def equal_time_comparison(ctx: api.Context, desc: SceneDesc, time_s: float = 4.0
         "guided": {"spp": guided_spp, "seconds": guided_t, "relmse": rg, "mse": float(np.mean((guided - ref) ** 2)),
                    "train_steps": guide.steps()},
         "relmse_ratio_plain_over_guided": rp / rg if rg > 0 else None,
+        "by_reference_luminance": luminance_breakdown(plain, guided, ref),
+        "network_time_share": share,
         "images": (plain, guided, ref),
     }
