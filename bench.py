@@ -56,7 +56,7 @@ NODE_BYTES, TRI_BYTES = 64, 48
 # dram__bytes_write.sum over the rays of one launch) from an ncu capture of the
 # terrain workload's extension launch; scaled to the average launch for
 # roofline.traffic.
-EXTEND_DRAM_BYTES_PER_RAY = 201.5
+EXTEND_DRAM_BYTES_PER_RAY = 179.1
 
 
 def wavefront_bytes(paths: int, ext: int, shadow: int) -> int:
