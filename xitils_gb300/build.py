@@ -28,7 +28,7 @@ UNITS = {
     "trace.cu": [],
     "integrator.cu": ["-fmad=false"],
     "noalloc.cu": [],
-    "guide.cu": [], "image.cu": [], "batch.cu": [],
+    "guide.cu": [], "guide_tc.cu": [], "image.cu": [], "batch.cu": [],
     "svndf.cu": ["-fmad=false"],
     "shade_layered.cu": ["-fmad=false"], "shade_nested.cu": ["-fmad=false"], "shade_batch_nested.cu": ["-fmad=false"],
 }

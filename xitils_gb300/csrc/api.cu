@@ -1413,6 +1413,7 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     }
     if (c.errors & ERR_STACK) return fail(ctx, XGB_QUEUE_OVERFLOW, "xgb_render: traversal stack overflow");
     if (c.errors & ERR_LOOP) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: traversal iteration bound exceeded");
+    if (c.errors & ERR_WAIT) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: guiding network inference wait timed out");
     return XGB_OK;
 }
 
@@ -1561,6 +1562,19 @@ float initUniform(uint64_t& state) {
 
 extern "C" {
 
+// Reads and clears the error word of the tensor-memory row inference (after the
+// stream has been synchronised); XGB_DEVICE_TIMEOUT when one of its waits gave up.
+static xgb_status guideRowErrors(xgb_guide* gd, const char* what) {
+    unsigned int e = 0;
+    unsigned int* word = reinterpret_cast<unsigned int*>(gd->g.scratch.scalars + 2);
+    if (cudaMemcpy(&e, word, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return fail(gd->ctx, XGB_CUDA_ERROR, what);
+    if (e & ERR_WAIT) {
+        cudaMemset(word, 0, 4);
+        return fail(gd->ctx, XGB_DEVICE_TIMEOUT, std::string(what) + ": network inference wait timed out");
+    }
+    return XGB_OK;
+}
+
 xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
     if (!ctx || !out) return XGB_INVALID_ARG;
     cudaSetDevice(ctx->device);
@@ -1632,7 +1646,7 @@ xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
     }
     cudaMemcpy(g.params, p.data(), 4 * kGuideParams, cudaMemcpyHostToDevice);
     guideRefresh(g, ctx->stream);
-    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    if (guideTcPrepare() != cudaSuccess || cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         for (void* q : gd->allocations) dfree(q);
         delete gd;
         return fail(ctx, XGB_CUDA_ERROR, "xgb_guide_create: initialisation failed");
@@ -1721,7 +1735,7 @@ xgb_status xgb_guide_infer(xgb_guide* gd, int n, const float* pos, const float* 
             std::memcpy(out + (size_t)(b + r) * kGuideOut, y.data() + (size_t)r * kGuideOutPad, 4 * kGuideOut);
     }
     cudaFree(dIn);
-    return XGB_OK;
+    return guideRowErrors(gd, "xgb_guide_infer");
 }
 
 xgb_status xgb_guide_sample(xgb_guide* gd, int n, const float* pos, const float* nrm, const float* wo, uint32_t seed,
@@ -1747,7 +1761,7 @@ xgb_status xgb_guide_sample(xgb_guide* gd, int n, const float* pos, const float*
     cudaError_t e = cudaStreamSynchronize(st);
     cudaFree(dIn);
     if (e != cudaSuccess) return cudaFail(ctx, e, "xgb_guide_sample");
-    return XGB_OK;
+    return guideRowErrors(gd, "xgb_guide_sample");
 }
 
 xgb_status xgb_guide_train_batch(xgb_guide* gd, int n, const float* pos, const float* nrm, const float* wo,

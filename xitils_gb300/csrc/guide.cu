@@ -1,6 +1,7 @@
 // Guiding network kernels: BF16 tensor-core (mma.sync m16n8k16, FP32
-// accumulation) inference and training of the 64-64-64-64-40 MLP, Adam, and
-// the per-path inference pass of the wavefront.
+// accumulation) training of the 64-64-64-64-40 MLP (forward, backward and the
+// weight gradients of a 64-row tile per warp group) and Adam. Inference, for
+// host rows and for the wavefront's paths, is in guide_tc.cu (tcgen05, TMEM).
 //
 // Layouts: activations are row-major bf16 [rows][64]; W_l is row-major bf16
 // [out][in] (out padded to 48 for the last layer) and WT_l its transpose
@@ -38,84 +39,6 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 
 // One dense layer for 16 rows held by a warp: out[16][N] = act(in[16][64] . W^T + b).
 // in: row stride ldi (elements); W: [N][64]; out written as bf16 (ldo) or fp32 (ldf).
-template <int N, bool RELU, bool OUT_F32>
-__device__ __forceinline__ void warpLayer(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* W, const float* bias,
-                                          __nv_bfloat16* outb, int ldo, float* outf, int ldf) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t a[4][4];
-#pragma unroll
-    for (int ks = 0; ks < 4; ++ks) {
-        a[ks][0] = ld32(in + g * ldi + ks * 16 + 2 * t);
-        a[ks][1] = ld32(in + (g + 8) * ldi + ks * 16 + 2 * t);
-        a[ks][2] = ld32(in + g * ldi + ks * 16 + 2 * t + 8);
-        a[ks][3] = ld32(in + (g + 8) * ldi + ks * 16 + 2 * t + 8);
-    }
-#pragma unroll
-    for (int nt = 0; nt < N / 8; ++nt) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-        const __nv_bfloat16* wr = W + (nt * 8 + g) * 64;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) mma16816(c, a[ks], ld32(wr + ks * 16 + 2 * t), ld32(wr + ks * 16 + 2 * t + 8));
-        const int col = nt * 8 + 2 * t;
-        float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
-        float v0 = c[0] + b0, v1 = c[1] + b1, v2 = c[2] + b0, v3 = c[3] + b1;
-        if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f); }
-        if (OUT_F32) {
-            outf[g * ldf + col] = v0; outf[g * ldf + col + 1] = v1;
-            outf[(g + 8) * ldf + col] = v2; outf[(g + 8) * ldf + col + 1] = v3;
-        } else {
-            *reinterpret_cast<uint32_t*>(outb + g * ldo + col) = pack2(v0, v1);
-            *reinterpret_cast<uint32_t*>(outb + (g + 8) * ldo + col) = pack2(v2, v3);
-        }
-    }
-}
-
-// warpLayer for 32 rows (two m16 tiles sharing every weight fragment): each
-// weight pair is loaded once per 32 rows instead of once per 16.
-template <int N, bool RELU, bool OUT_F32>
-__device__ __forceinline__ void warpLayer32(const __nv_bfloat16* in, int ldi, const __nv_bfloat16* W, const float* bias,
-                                            __nv_bfloat16* outb, int ldo, float* outf, int ldf) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t a[2][4][4];
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-            const __nv_bfloat16* r0 = in + (16 * m + g) * ldi + ks * 16 + 2 * t;
-            const __nv_bfloat16* r1 = r0 + 8 * ldi;
-            a[m][ks][0] = ld32(r0);
-            a[m][ks][1] = ld32(r1);
-            a[m][ks][2] = ld32(r0 + 8);
-            a[m][ks][3] = ld32(r1 + 8);
-        }
-#pragma unroll
-    for (int nt = 0; nt < N / 8; ++nt) {
-        float c[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-        const __nv_bfloat16* wr = W + (nt * 8 + g) * 64;
-#pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-            const uint32_t b0 = ld32(wr + ks * 16 + 2 * t), b1 = ld32(wr + ks * 16 + 2 * t + 8);
-            mma16816(c[0], a[0][ks], b0, b1);
-            mma16816(c[1], a[1][ks], b0, b1);
-        }
-        const int col = nt * 8 + 2 * t;
-        const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-            float v0 = c[m][0] + b0, v1 = c[m][1] + b1, v2 = c[m][2] + b0, v3 = c[m][3] + b1;
-            if (RELU) { v0 = fmaxf(v0, 0.f); v1 = fmaxf(v1, 0.f); v2 = fmaxf(v2, 0.f); v3 = fmaxf(v3, 0.f); }
-            const int r0 = 16 * m + g, r1 = r0 + 8;
-            if (OUT_F32) {
-                outf[r0 * ldf + col] = v0; outf[r0 * ldf + col + 1] = v1;
-                outf[r1 * ldf + col] = v2; outf[r1 * ldf + col + 1] = v3;
-            } else {
-                *reinterpret_cast<uint32_t*>(outb + r0 * ldo + col) = pack2(v0, v1);
-                *reinterpret_cast<uint32_t*>(outb + r1 * ldo + col) = pack2(v2, v3);
-            }
-        }
-    }
-}
-
 // --------------------------------------------------------------- training --
 // One Adam step is two launches.
 //   k_trainTiles: a CTA takes 64-row tiles of the batch (4 warps x 16 rows) and
@@ -443,33 +366,11 @@ __global__ void k_refreshBf16(const float* params, GuideWeights w) {
     if (i < kGuideParams) guideStoreBf16(w, i, params[i]);
 }
 
-// Fused inference for host-supplied feature rows (API / tests): X0 [rows][64] bf16 -> Y [rows][48] fp32.
-__global__ void k_inferRows(const __nv_bfloat16* X0, int rows, GuideWeights w, float* Y) {
-    __shared__ __align__(16) __nv_bfloat16 buf[4][2][16 * 72];
-    const int warpInBlock = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= rows / 16) return;
-    const size_t r0 = (size_t)warp * 16;
-    __nv_bfloat16* s0 = buf[warpInBlock][0];
-    __nv_bfloat16* s1 = buf[warpInBlock][1];
-    warpLayer<64, true, false>(X0 + r0 * 64, 64, w.W[0], w.bias[0], s0, 72, nullptr, 0);
-    __syncwarp();
-    warpLayer<64, true, false>(s0, 72, w.W[1], w.bias[1], s1, 72, nullptr, 0);
-    __syncwarp();
-    warpLayer<64, true, false>(s1, 72, w.W[2], w.bias[2], s0, 72, nullptr, 0);
-    __syncwarp();
-    warpLayer<kGuideOutPad, false, true>(s0, 72, w.W[3], w.bias[3], nullptr, 0, Y + r0 * kGuideOutPad, kGuideOutPad);
-}
 }  // namespace
 
 // ------------------------------------------------------------- host side --
 void guideRefresh(const GuideDevice& g, cudaStream_t s) {
     k_refreshBf16<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g.params, g.w);
-}
-
-void guideInferRows(const GuideDevice& g, const __nv_bfloat16* X0, int rowsPad, float* Y, cudaStream_t s) {
-    int warps = rowsPad / 16;
-    k_inferRows<<<(warps + 3) / 4, 128, 0, s>>>(X0, rowsPad, g.w, Y);
 }
 
 void guideTrainStep(GuideDevice& g, const GuideRecord* rec, int n, GuideBounds gb, float lr, cudaStream_t s) {
@@ -582,67 +483,6 @@ __global__ void k_pointFeatures(const float* p, const float* n, const float* wo,
     for (int i = 0; i < 64; i += 2) *reinterpret_cast<uint32_t*>(x + i) = pack2(f[i], f[i + 1]);
 }
 
-// Per-path inference: every hit of the input queue gets its 8-lobe mixture
-// (10 float4: lobes' (mu, kappa) then the 8 weights). A warp takes 32 paths, one
-// per lane: the lane reconstructs its hit, writes its 64 features into the warp's
-// activation rows, and decodes its own output row; the four layers run as two
-// m16 tiles over the 32 rows (warpLayer32).
-__global__ void __launch_bounds__(128, 4) k_inferPaths(SceneDev sc, GuideWeights w, GuideBounds gb, PathQueue q, HitQueue h,
-                                                    const Ctrl* ctrl, float4* mix) {
-    __shared__ __align__(16) __nv_bfloat16 act[4][2][32 * 72];
-    __shared__ float outY[4][32 * kGuideOutPad];
-    const unsigned int n = ctrl->nActive;
-    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned int warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const unsigned int nWarps = (gridDim.x * blockDim.x) >> 5;
-    for (unsigned int base = warpGlobal * 32u; base < n; base += nWarps * 32u) {
-        const unsigned int i = base + lane;
-        __nv_bfloat16* x = act[wib][0] + lane * 72;
-        bool valid = false;
-        if (i < n) {
-            const float4 hh = h.h[i];
-            const int prim = __float_as_int(hh.w);
-            if (prim >= 0) {
-                const float4 d4 = q.d[i];
-                const Surface s = makeSurface(sc, sc.instances[h.inst[i]], prim, hh.y, hh.z, V3(d4.x, d4.y, d4.z));
-                const float pf[3] = {(s.p.x - gb.lo[0]) * gb.invExtent[0], (s.p.y - gb.lo[1]) * gb.invExtent[1],
-                                     (s.p.z - gb.lo[2]) * gb.invExtent[2]};
-                const float nf[3] = {s.sn.x, s.sn.y, s.sn.z}, wf[3] = {s.wo.x, s.wo.y, s.wo.z};
-                float f[64];
-                guideFeatures(pf, nf, wf, f);
-#pragma unroll
-                for (int k = 0; k < 64; k += 2) *reinterpret_cast<uint32_t*>(x + k) = pack2(f[k], f[k + 1]);
-                valid = true;
-            }
-        }
-        if (!valid)
-#pragma unroll
-            for (int k = 0; k < 64; k += 2) *reinterpret_cast<uint32_t*>(x + k) = 0u;
-        __syncwarp();
-        warpLayer32<64, true, false>(act[wib][0], 72, w.W[0], w.bias[0], act[wib][1], 72, nullptr, 0);
-        __syncwarp();
-        warpLayer32<64, true, false>(act[wib][1], 72, w.W[1], w.bias[1], act[wib][0], 72, nullptr, 0);
-        __syncwarp();
-        warpLayer32<64, true, false>(act[wib][0], 72, w.W[2], w.bias[2], act[wib][1], 72, nullptr, 0);
-        __syncwarp();
-        warpLayer32<kGuideOutPad, false, true>(act[wib][1], 72, w.W[3], w.bias[3], nullptr, 0, outY[wib], kGuideOutPad);
-        __syncwarp();
-        if (i < n) {
-            VmfMixture mx;
-            decodeMixture(outY[wib] + lane * kGuideOutPad, mx);
-            float4* o = mix + (size_t)i * 10;
-#pragma unroll
-            for (int j = 0; j < kGuideLobes; ++j)
-                __stcs(o + j, make_float4(mx.lobe[j].mu.x, mx.lobe[j].mu.y, mx.lobe[j].mu.z, mx.lobe[j].kappa));
-            __stcs(o + 8, make_float4(mx.lobe[0].alpha, mx.lobe[1].alpha, mx.lobe[2].alpha, mx.lobe[3].alpha));
-            __stcs(o + 9, make_float4(mx.lobe[4].alpha, mx.lobe[5].alpha, mx.lobe[6].alpha, mx.lobe[7].alpha));
-        }
-        __syncwarp();
-    }
-}
-}  // namespace
-
-namespace {
 __global__ void k_sampleRows(const float* Y, int n, uint32_t seed, float* dirs, float* pdf) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
@@ -663,11 +503,6 @@ void guideSampleRows(const float* Y, int n, uint32_t seed, float* dirs, float* p
 void guideFeaturesFromPoints(const float* p, const float* n, const float* wo, int count, int rowsPad, GuideBounds gb,
                              __nv_bfloat16* X0, cudaStream_t s) {
     k_pointFeatures<<<(rowsPad + 127) / 128, 128, 0, s>>>(p, n, wo, count, rowsPad, gb, X0);
-}
-
-void guideInferPaths(const SceneDev& sc, const GuideDevice& g, GuideBounds gb, PathQueue q, HitQueue h, const Ctrl* ctrl,
-                     float4* mix, int grid, cudaStream_t s) {
-    k_inferPaths<<<grid, 128, 0, s>>>(sc, g.w, gb, q, h, ctrl, mix);
 }
 
 }  // namespace xgb

@@ -22,7 +22,8 @@ struct GuideScratch {
     __nv_bfloat16* X0;  // feature rows [rows][64] of the inference entry points
     float* Y;           // outputs [rows][48]
     float* partial;     // per-CTA partial gradients of a training step (guidePartialBytes())
-    float* scalars;     // [0] total sample weight, [1] loss of the last training step
+    float* scalars;     // [0] total sample weight, [1] loss of the last training step,
+                        // [2] (as unsigned int) ERR_WAIT of the tensor-memory row inference
 };
 
 struct GuideDevice {
@@ -44,6 +45,8 @@ struct GuideDevice {
 __device__ void guideStoreBf16(const GuideWeights& w, int i, float p);
 
 void guideRefresh(const GuideDevice& g, cudaStream_t s);
+// Network outputs Y [rowsPad][48] of feature rows X0 [rowsPad][64] (tcgen05 kernel of
+// guide_tc.cu); a timed-out wait sets ERR_WAIT in the word at g.scratch.scalars + 2.
 void guideInferRows(const GuideDevice& g, const __nv_bfloat16* X0, int rowsPad, float* Y, cudaStream_t s);
 // Bytes of GuideScratch::partial.
 size_t guidePartialBytes();
@@ -64,8 +67,12 @@ void guideFeaturesFromPoints(const float* p, const float* n, const float* wo, in
                              __nv_bfloat16* X0, cudaStream_t s);
 // Directions drawn from decoded output rows (Y [n][48]) and their mixture pdf.
 void guideSampleRows(const float* Y, int n, uint32_t seed, float* dirs, float* pdf, cudaStream_t s);
-// Per-path inference for the wavefront: mixture (10 float4 per path) for every hit in q[0, nActive).
-void guideInferPaths(const SceneDev& sc, const GuideDevice& g, GuideBounds gb, PathQueue q, HitQueue h, const Ctrl* ctrl,
+// Per-path inference for the wavefront: mixture (10 float4 per path) for every hit in q[0, nActive);
+// a timed-out wait of the tensor-memory kernel sets ERR_WAIT in ctrl->errors.
+void guideInferPaths(const SceneDev& sc, const GuideDevice& g, GuideBounds gb, PathQueue q, HitQueue h, Ctrl* ctrl,
                      float4* mix, int grid, cudaStream_t s);
+// Sets the dynamic shared-memory limit of the tensor-memory inference kernels
+// and sizes their grid (once per process, on the current device).
+cudaError_t guideTcPrepare();
 
 }  // namespace xgb

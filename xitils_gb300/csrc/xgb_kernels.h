@@ -63,7 +63,8 @@ struct Ctrl {
     unsigned long long triTests;
 };
 
-enum ErrorBits : unsigned int { ERR_STACK = 1u, ERR_QUEUE = 2u, ERR_LOOP = 4u };
+// ERR_WAIT: a bounded mbarrier wait of the tensor-memory inference kernels gave up.
+enum ErrorBits : unsigned int { ERR_STACK = 1u, ERR_QUEUE = 2u, ERR_LOOP = 4u, ERR_WAIT = 8u };
 
 struct PathQueue {
     float4* o;          // o.xyz, w = pdf of the BSDF sample that produced this ray (-1: specular)
