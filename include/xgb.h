@@ -63,6 +63,16 @@ xgb_status xgb_ctx_set_bvh_layout(xgb_ctx* ctx, int layout);
  * changes speed only. The reference renders 16 x 16 tiles on OpenMP threads
  * (Include/Xitils/RenderTarget.h:58-59, :110-113). */
 xgb_status xgb_ctx_set_path_order(xgb_ctx* ctx, int tile_w, int tile_h);
+/* Sample order of this context's renders: with samples > 1, consecutive camera
+ * paths are `samples` consecutive samples of one pixel (passes of that many
+ * samples over the film, the remainder of a call's samples one pass after the
+ * other); 0 or 1 = one sample pass over the film after the other. Default 64:
+ * a warp's camera rays then leave one or a few pixels, traverse the same nodes
+ * and reuse them in L1 and L2. Every
+ * (pixel, sample) keeps its own random stream, so this changes speed only. The
+ * reference renders one 16 x 16 tile per thread, the tile's pixels once per
+ * sample, sample after sample (Include/Xitils/RenderTarget.h:108-127). */
+xgb_status xgb_ctx_set_sample_grouping(xgb_ctx* ctx, int samples);
 /* Waits for the work enqueued on stream (NULL = the context's own stream). */
 xgb_status xgb_ctx_synchronize(xgb_ctx* ctx, void* stream);
 /* Last error message of this context ("" when none). Never NULL. */

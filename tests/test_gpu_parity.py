@@ -205,3 +205,39 @@ def test_tiled_path_order_same_image(ctx):
     for tw, th in ((0, 4), (-1, -1), (257, 1)):
         with pytest.raises(api.XgbError):
             ctx.set_path_order(tw, th)
+
+
+def test_sample_grouping_same_image(ctx):
+    """Camera paths as runs of consecutive samples of one pixel
+    (xgb_ctx_set_sample_grouping): every (pixel, sample) keeps its random stream,
+    so the film equals the sample-pass order's up to the order of the FP32
+    additions; group sizes that divide the call's samples, ones that leave a
+    remainder, ones larger than the call, and a call that starts at sample 3."""
+    from xitils_gb300 import api
+    desc = scenes.cornell(40, 30, 6)
+    b = api.load_scene(ctx, desc)
+    for begin in (0, 3):
+        ctx.set_sample_grouping(0)
+        base = api.RenderTarget(ctx, desc.width, desc.height)
+        base.render(b.scene, desc.spp, desc.params, begin)
+        want = base.download()
+        try:
+            for g in (2, 3, 4, 8, 64):
+                ctx.set_sample_grouping(g)
+                rt = api.RenderTarget(ctx, desc.width, desc.height)
+                rt.render(b.scene, desc.spp, desc.params, begin)
+                np.testing.assert_allclose(rt.download(), want, rtol=1e-5, atol=1e-6, err_msg=f"group {g}, begin {begin}")
+                st = b.scene.stats()
+                assert st["paths"] == desc.n_paths and st["error_flags"] == 0
+        finally:
+            ctx.set_sample_grouping()
+    cpu = load_cpu(desc, "port").render_pcg(desc)
+    ctx.set_sample_grouping(4)
+    try:
+        gpu = api.render_desc(ctx, desc)
+    finally:
+        ctx.set_sample_grouping()
+    assert relmse(gpu, cpu) <= TOL
+    for g in (-1, 4097):
+        with pytest.raises(api.XgbError):
+            ctx.set_sample_grouping(g)

@@ -74,6 +74,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_ctx_set_bvh_builder": [P, C.c_int],
         "xgb_ctx_set_bvh_layout": [P, C.c_int],
         "xgb_ctx_set_path_order": [P, C.c_int, C.c_int],
+        "xgb_ctx_set_sample_grouping": [P, C.c_int],
         "xgb_scene_intersect": [P, C.c_int, FP, FP, P],
         "xgb_scene_occluded": [P, C.c_int, FP, C.POINTER(C.c_int32), P],
         "xgb_film_enable_aovs": [P],
@@ -200,6 +201,11 @@ class Context:
     def set_path_order(self, tile_w: int = 0, tile_h: int = 0):
         """Camera paths in tile_w x tile_h pixel blocks (0, 0 = scanline rows); speed only."""
         self.check(self.lib.xgb_ctx_set_path_order(self.h, int(tile_w), int(tile_h)), "set_path_order")
+
+    def set_sample_grouping(self, samples: int = 64):
+        """Camera paths as runs of `samples` consecutive samples of one pixel (the
+        default 64; 0 = one sample pass over the film after the other); speed only."""
+        self.check(self.lib.xgb_ctx_set_sample_grouping(self.h, int(samples)), "set_sample_grouping")
 
     def synchronize(self, stream=None):
         self.check(self.lib.xgb_ctx_synchronize(self.h, stream), "synchronize")

@@ -95,6 +95,10 @@ struct xgb_ctx {
     int bvhBuilder = kBuilderPloc;
     int bvhLayout = kLayoutBinary;
     int tileW = 0, tileH = 0;  // camera-path order (xgb_ctx_set_path_order)
+    // consecutive samples of a pixel among the camera paths (xgb_ctx_set_sample_grouping);
+    // 64 by default: the terrain's 64-spp render took 44.8 ms in sample passes, 38.5 ms
+    // in runs of 32 samples, 38.1 ms in runs of 64
+    int sampleGroup = 64;
 };
 
 struct xgb_texture {
@@ -281,6 +285,14 @@ xgb_status xgb_ctx_set_path_order(xgb_ctx* ctx, int tile_w, int tile_h) {
         return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_path_order: tile sides in [1, 256], or both 0");
     ctx->tileW = tile_w;
     ctx->tileH = tile_h;
+    return XGB_OK;
+}
+
+xgb_status xgb_ctx_set_sample_grouping(xgb_ctx* ctx, int samples) {
+    if (!ctx) return XGB_INVALID_ARG;
+    if (samples < 0 || samples > 4096)
+        return fail(ctx, XGB_INVALID_ARG, "xgb_ctx_set_sample_grouping: samples in [0, 4096]");
+    ctx->sampleGroup = samples;
     return XGB_OK;
 }
 
@@ -1257,6 +1269,8 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
     rp.dropNonFinite = (s->fixes & XGB_FIX_DROP_NONFINITE) ? 1 : 0;
     rp.tileW = ctx->tileW;
     rp.tileH = ctx->tileH;
+    rp.sampleGroup = ctx->sampleGroup;
+    rp.sppCount = spp_count;
     rp.guided = 0;
     rp.train = 0;
     rp.bsdfFrac = s->bsdfFrac;
@@ -1534,6 +1548,7 @@ void renderExtras(const xgb_scene* s, const xgb_film* f, int* filmAovs, int* sce
     *sceneGuide = (s && s->guide) ? 1 : 0;
 }
 xgb_ctx* sceneContext(xgb_scene* s) { return s ? s->ctx : nullptr; }
+int sampleGrouping(const xgb_ctx* ctx) { return ctx ? ctx->sampleGroup : 0; }
 xgb_status contextFail(xgb_ctx* ctx, xgb_status st, const std::string& msg) { return fail(ctx, st, msg); }
 bool filmPlane(xgb_film* f, void** d, int* w, int* h, int* fp64, int* device, cudaStream_t* ctxStream) {
     if (!f) return false;

@@ -31,6 +31,7 @@ namespace xgb {
 bool sceneView(xgb_scene* s, SceneDev* sd, int* device, int* numSMs, cudaStream_t* stream, int* built);
 bool filmPlane(xgb_film* f, void** d, int* w, int* h, int* fp64, int* device, cudaStream_t* ctxStream);
 xgb_ctx* sceneContext(xgb_scene* s);
+int sampleGrouping(const xgb_ctx* ctx);
 xgb_status contextFail(xgb_ctx* ctx, xgb_status st, const std::string& msg);
 }  // namespace xgb
 
@@ -181,6 +182,8 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
         RenderParams rp{};
         rp.width = w; rp.height = h;
         rp.sppBegin = jobs[i].spp_begin;
+        rp.sampleGroup = sampleGrouping(ctx);
+        rp.sppCount = jobs[i].spp_count;
         rp.seed = P.seed;
         rp.integrator = P.integrator;
         rp.maxDepth = P.max_depth;

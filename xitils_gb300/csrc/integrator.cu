@@ -62,6 +62,27 @@ __device__ __forceinline__ unsigned int tiledPixel(unsigned int i, unsigned int 
     return x + y * W;
 }
 
+// Sample and pixel index of the call's local-th camera path when groups of G
+// consecutive paths are G samples of one pixel: passes of G samples over the
+// film, then (when G does not divide the call's sample count) the remaining
+// samples one pass after the other. Bijective on [0, px spp).
+__device__ __forceinline__ void groupedSample(unsigned long long local, unsigned int px, unsigned int spp,
+                                              unsigned int G, unsigned int& sample, unsigned int& pix) {
+    const unsigned int full = (spp / G) * G;
+    const unsigned long long grouped = (unsigned long long)full * px;
+    if (local < grouped) {
+        const unsigned long long pass = (unsigned long long)px * G;
+        const unsigned int grp = (unsigned int)(local / pass);
+        const unsigned int r = (unsigned int)(local - (unsigned long long)grp * pass);
+        pix = r / G;
+        sample = grp * G + r % G;
+    } else {
+        const unsigned long long t = local - grouped;
+        sample = full + (unsigned int)(t / px);
+        pix = (unsigned int)(t % px);
+    }
+}
+
 template <class J>
 __global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, const Ctrl* ctrl) {
     const unsigned int nCont = ctrl->nCont, nActive = ctrl->nActive;
@@ -73,8 +94,14 @@ __global__ void __launch_bounds__(kShadeBlock) k_generate(J jobs, PathQueue q, c
         const SceneDev& sc = jobs.scene(job);
         const RenderParams& rp = jobs.params(job);
         const unsigned int px = (unsigned int)rp.width * (unsigned int)rp.height;
-        unsigned int sample = rp.sppBegin + (unsigned int)(local / px);
-        unsigned int pix = (unsigned int)(local % px);
+        unsigned int sample, pix;
+        if (rp.sampleGroup > 1 && rp.sppCount > 1) {
+            groupedSample(local, px, rp.sppCount, min((unsigned int)rp.sampleGroup, rp.sppCount), sample, pix);
+            sample += rp.sppBegin;
+        } else {
+            sample = rp.sppBegin + (unsigned int)(local / px);
+            pix = (unsigned int)(local % px);
+        }
         if (rp.tileW > 0) pix = tiledPixel(pix, (unsigned int)rp.width, (unsigned int)rp.height, (unsigned int)rp.tileW,
                                            (unsigned int)rp.tileH);
         int x = (int)(pix % (unsigned int)rp.width), y = (int)(pix / (unsigned int)rp.width);

@@ -38,6 +38,8 @@ namespace xgb {
 bool sceneView(xgb_scene* s, SceneDev* sd, int* device, int* numSMs, cudaStream_t* stream, int* built);
 bool filmView(xgb_film* f, const xgb_scene* s, void** d, int* w, int* h, int* fp64);
 void renderExtras(const xgb_scene* s, const xgb_film* f, int* filmAovs, int* sceneGuide);
+xgb_ctx* sceneContext(xgb_scene* s);
+int sampleGrouping(const xgb_ctx* ctx);
 }  // namespace xgb
 
 using namespace xgb;
@@ -128,6 +130,8 @@ extern "C" xgb_status xgb_render_noalloc(xgb_scene* scene, const xgb_integrator_
     RenderParams rp{};  // learned-proposal fields stay off (0 / nullptr)
     rp.width = W; rp.height = H;
     rp.sppBegin = spp_begin;
+    rp.sampleGroup = sampleGrouping(sceneContext(scene));
+    rp.sppCount = spp_count;
     rp.seed = P.seed;
     rp.integrator = P.integrator;
     rp.maxDepth = P.max_depth;

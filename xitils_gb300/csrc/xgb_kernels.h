@@ -134,6 +134,12 @@ struct RenderParams {
     // order of the camera paths of a sample pass: tileW x tileH pixel blocks
     // (k_generate), 0 = scanline rows
     int tileW, tileH;
+    // order of the samples: sampleGroup (> 1) consecutive camera paths are
+    // consecutive samples of one pixel, in passes of sampleGroup samples over
+    // the film; 0 or 1 = one sample pass over the film after the other.
+    // sppCount = samples of this call.
+    int sampleGroup;
+    unsigned int sppCount;
 };
 
 // Device arrays of a batch of render jobs sharing one wavefront (xgb_render_batch):
