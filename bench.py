@@ -52,11 +52,12 @@ L2_BYTES = 129 * 1024 * 1024
 EXTEND_BYTES_PER_RAY = 52
 # BVH traffic per visit (reported against L2, not HBM): 64 B node, 48 B triangle.
 NODE_BYTES, TRI_BYTES = 64, 48
-# DRAM bytes per extension ray of k_trace_single (dram__bytes_read.sum +
-# dram__bytes_write.sum over the rays of one launch) from an ncu capture of the
-# terrain workload's extension launch; scaled to the average launch for
+# DRAM bytes per extension ray of k_trace_single: dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the 24 closest-hit launches of one terrain
+# render (6.98 GB for 119,571,102 rays, camera paths in runs of 64 samples of a
+# pixel), from a one-pass ncu capture; scaled to the average launch for
 # roofline.traffic.
-EXTEND_DRAM_BYTES_PER_RAY = 179.1
+EXTEND_DRAM_BYTES_PER_RAY = 58.4
 
 
 def wavefront_bytes(paths: int, ext: int, shadow: int) -> int:

@@ -78,3 +78,36 @@ def test_autotune_picks_a_candidate_and_caches_it(setup):
     assert api.batch_stats(ctx)["paths"] == sum(d.width * d.height * d.spp for d in descs)
     for (_, rt, _, _, _), d in zip(jobs, descs):
         assert rt.download().sum() > 0
+
+
+def test_batch_of_one_instance_scenes(setup):
+    """A batch whose every job is one instance of a binary mesh BVH runs the
+    one-instance traversal kernel with a per-ray mesh (k_trace_single over
+    BatchScenes): terrains of three sizes and a transformed, textured-sky box,
+    each film equal to its single render."""
+    import math
+    from xitils_gb300.scene import SKY_UNIFORM, SceneDesc
+    from xitils_gb300.scenes import look_at, transformTRS, unit_cube_mesh
+    api, ctx, _, _ = setup
+    box = SceneDesc(name="one box", width=40, height=24, spp=4,
+                    params=IntegratorParams(max_depth=5, rr_start=3, rr_prob=0.8, seed=5))
+    cpos, cidx = unit_cube_mesh()
+    box.add_object(box.add_mesh(cpos, cidx), box.metal(0.3, [0.9, 0.6, 0.3]),
+                   transformTRS((0.1, -0.2, 0.3), (0.0, 35.0, 0.0), (0.8, 1.3, 0.6)))
+    box.set_sky(SKY_UNIFORM, rgb=[0.8, 0.9, 1.0])
+    box.set_camera(look_at((2.0, 1.5, -2.5), (0.0, 0.0, 0.0), (0, 1, 0)), 45.0 * math.pi / 180.0, 24 / 40)
+    descs = [scenes.terrain(grid=g, width=w, height=h, spp=2, env_size=(64, 32))
+             for g, w, h in ((17, 24, 16), (65, 48, 32), (129, 32, 32))] + [box]
+    builders = [api.load_scene(ctx, d) for d in descs]
+    jobs, expect = [], []
+    for k, (d, b) in enumerate(zip(descs, builders)):
+        rt = api.RenderTarget(ctx, d.width, d.height)
+        jobs.append((b.scene, rt, d.params, 2 * k, d.spp))
+        expect.append(_single(api, ctx, d, b, d.params, 2 * k, d.spp))
+    api.render_batch(ctx, jobs, queue_capacity=4096, iterations_per_sync=4, use_graph=True)
+    st = api.batch_stats(ctx)
+    assert st["paths"] == sum(d.width * d.height * d.spp for d in descs) and st["error_flags"] == 0
+    for d, (_, rt, _, _, _), e in zip(descs, jobs, expect):
+        got = rt.download()
+        assert np.isfinite(got).all() and got.sum() > 0
+        np.testing.assert_allclose(got, e, rtol=1e-5, atol=1e-5 * max(1.0, float(np.abs(e).max())), err_msg=d.name)

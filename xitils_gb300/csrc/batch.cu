@@ -170,11 +170,12 @@ std::string shapeKey(const xgb_batch_job* jobs, int n) {
 xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int n, const xgb_batch_options& o,
                     cudaStream_t st, int device, int numSMs, double* seconds) {
     unsigned long long total = 0;
-    int flat = 1, nested = 0;
+    int flat = 1, single = 1, nested = 0;
     for (int i = 0; i < n; ++i) {
         SceneDev sd; int dev, sms, built; cudaStream_t cs;
         sceneView(jobs[i].scene, &sd, &dev, &sms, &cs, &built);
         if (sd.nInstances > 16 || sd.blasLayout != 0 || sd.shell) flat = 0;
+        if (sd.nInstances != 1 || sd.blasLayout != 0 || sd.shell) single = 0;
         nested |= sd.nested ? 1 : 0;
         void* fd; int w, h, f64, fdev; cudaStream_t fcs;
         filmPlane(jobs[i].film, &fd, &w, &h, &f64, &fdev, &fcs);
@@ -214,8 +215,9 @@ xgb_status runBatch(xgb_ctx* ctx, BatchState* b, const xgb_batch_job* jobs, int 
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->dStart, b->hStart, sizeof(unsigned long long) * (n + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctrl, b->ctrlHost, sizeof(Ctrl), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return contextFail(ctx, XGB_CUDA_ERROR, std::string("xgb_render_batch: ") + cudaGetErrorString(e));
-    const BatchView v{b->dScenes, b->dParams, b->dStart, n, flat, nested};
-    const int kernels = flat | (nested << 1);  // which kernels a captured graph holds
+    const int layout = single ? kBatchSingle : flat ? kBatchFlat : 0;
+    const BatchView v{b->dScenes, b->dParams, b->dStart, n, layout, nested};
+    const int kernels = layout | (nested << 2);  // which kernels a captured graph holds
     const int iters = std::max(2, (o.iterations_per_sync + 1) & ~1);
     const auto t0 = std::chrono::steady_clock::now();
     uint64_t launches = 0;

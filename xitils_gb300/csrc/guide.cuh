@@ -90,14 +90,17 @@ __device__ __forceinline__ float clampLogKappa(float k) {
 // Network output row (40 floats) -> mixture (softmax weights, exp kappa, unit mu).
 __device__ __forceinline__ void decodeMixture(const float* y, VmfMixture& mx) {
     float mxl = -1e30f;
+#pragma unroll
     for (int j = 0; j < kGuideLobes; ++j) mxl = fmaxf(mxl, y[5 * j + 4]);
     float sum = 0.0f;
+#pragma unroll
     for (int j = 0; j < kGuideLobes; ++j) {
         float e = __expf(y[5 * j + 4] - mxl);
         mx.lobe[j].alpha = e;
         sum += e;
     }
     float inv = 1.0f / sum;
+#pragma unroll
     for (int j = 0; j < kGuideLobes; ++j) {
         V3 m(y[5 * j], y[5 * j + 1], y[5 * j + 2]);
         float l2 = dot(m, m);

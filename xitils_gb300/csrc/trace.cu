@@ -9,6 +9,8 @@
 #include "trace.cuh"
 #include "xgb_kernels.h"
 
+#include <type_traits>
+
 namespace xgb {
 
 __device__ __forceinline__ void filmAdd(const RenderParams& rp, int pix, V3 c) {
@@ -507,14 +509,34 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
 // Ten blocks per SM (48 registers, no spills) rather than the nine that 55 registers
 // allow: the terrain's traversal ran 2.5 % faster; twelve (40 registers) spill and
 // ran 7 % slower.
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, RenderParams rp, PathQueue q, HitQueue h,
-                                                              ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+//
+// S = OneScene: the mesh, its instance transform and the bounds are the kernel's
+// constants. S = BatchScenes: every job of the batch is a one-instance scene with
+// a binary mesh BVH; a lane loads its ray's mesh when it fetches the ray (the job
+// in the high bits of the pixel field), at eight blocks per SM for the registers
+// that takes.
+template <class S>
+struct SingleTraits {
+    static constexpr int kMinBlocks = 10;
+};
+template <>
+struct SingleTraits<BatchScenes> {
+    static constexpr int kMinBlocks = 8;
+};
+
+template <bool ANY, bool COUNT, class S>
+__global__ void __launch_bounds__(kTraceBlock, SingleTraits<S>::kMinBlocks)
+    k_trace_single(S scenes, PathQueue q, HitQueue h, ShadowQueue s, PathQueue out, Ctrl* ctrl) {
+    constexpr bool kBatch = !std::is_same<S, OneScene>::value;
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
     unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
-    const Instance& in = sc.instances[0];
-    const MeshDev m = sc.meshes[in.mesh];
-    const bool identity = in.identity != 0;
+    // one scene: its only mesh for every ray; a batch: the current ray's
+    const Instance* in0 = kBatch ? nullptr : &scenes.scene(0).instances[0];
+    const bool identity0 = kBatch ? true : in0->identity != 0;
+    const MeshDev m0 = kBatch ? MeshDev{} : scenes.scene(0).meshes[in0->mesh];
+    const Node2* nodes = m0.nodes2;
+    const TriV* tris = m0.tris;
+    int job = 0;
     const int lane = threadIdx.x & 31;
     const unsigned int ltMask = (1u << lane) - 1u;
     int stack[kStackDepth];
@@ -543,9 +565,16 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             if (ANY) { o4 = __ldcs(&s.o[ray]); d4 = __ldcs(&s.d[ray]); tMax = o4.w; }
             else { o4 = __ldcs(&q.o[ray]); d4 = __ldcs(&q.d[ray]); tMax = __int_as_float(0x7f800000); }
             V3 o(o4.x, o4.y, o4.z), d(d4.x, d4.y, d4.z);
+            const Instance* in = in0;
+            bool identity = identity0;
+            if (kBatch) {
+                job = scenes.jobOf(ANY ? __float_as_uint(d4.w) : __float_as_uint(__ldg(&q.thr[ray].w)));
+                in = &scenes.scene(job).instances[0];
+                identity = in->identity != 0;
+            }
             if (!identity) {
-                o = xformPointRn(in.matInv, o);
-                d = xformVectorRn(in.matInv, d);
+                o = xformPointRn(in->matInv, o);
+                d = xformVectorRn(in->matInv, d);
             }
             r = makeWRay(o, d);
             hit.prim = -1;
@@ -553,14 +582,22 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             occluded = false;
             sp = 0;
             guard = 0;
-            if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
+            int rootIsLeaf = m0.rootIsLeaf, rootLeaf = m0.rootLeaf;
+            if (kBatch) {
+                const MeshDev& m = scenes.scene(job).meshes[in->mesh];
+                nodes = m.nodes2;
+                tris = m.tris;
+                rootIsLeaf = m.rootIsLeaf;
+                rootLeaf = m.rootLeaf;
+            }
+            if (rootIsLeaf) { leafAddr = rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > sc.maxSteps) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
+        if (guard > scenes.scene(job).maxSteps) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
         bool searching = true;
         while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
             if (COUNT) wc.nodes++;
-            const Node2* nd = m.nodes2 + nodeAddr;
+            const Node2* nd = nodes + nodeAddr;
             float4 a = __ldg(&nd->a), b = __ldg(&nd->b), c = __ldg(&nd->c);
             int4 dd = __ldg(&nd->d);
             float t0, t1;
@@ -569,7 +606,7 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= sc.stackLimit) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
+                if (sp >= scenes.scene(job).stackLimit) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
                 stack[sp++] = far;
                 nodeAddr = near;
             } else if (h0) {
@@ -590,7 +627,7 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             int first = leafFirst(leafAddr), cnt = leafCount(leafAddr);
             if (COUNT) wc.tris += cnt;
             for (int k = 0; k < cnt; ++k) {
-                const TriV* tv = m.tris + first + k;
+                const TriV* tv = tris + first + k;
                 float4 p0 = __ldg(&tv->p0), p1 = __ldg(&tv->p1), p2 = __ldg(&tv->p2);
                 float t, b0, b1;
                 if (watertight(r, p0, p1, p2, tMax, t, b0, b1)) {
@@ -608,7 +645,8 @@ __global__ void __launch_bounds__(kTraceBlock, 10) k_trace_single(SceneDev sc, R
             if (ANY) {
                 if (!occluded) {
                     float4 cc = s.c[ray];
-                    filmAdd(rp, __float_as_int(s.d[ray].w), V3(cc.x, cc.y, cc.z));
+                    const RenderParams& rp = scenes.params(job);
+                    filmAdd(rp, scenes.pixelOf(__float_as_uint(s.d[ray].w)), V3(cc.x, cc.y, cc.z));
                     int target = __float_as_int(cc.w);
                     if (target >= 0) out.rng[target] = s.rng[ray];
                     if (rp.train) creditPath(rp, s.pid[ray], cc);
@@ -748,8 +786,8 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
         if (count) XGB_LAUNCH((k_trace_wide<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_wide<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (sc.nInstances == 1 && sc.blasLayout == 0) {
-        if (count) XGB_LAUNCH((k_trace_single<false, true>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
-        else XGB_LAUNCH((k_trace_single<false, false>))(sc, none, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        if (count) XGB_LAUNCH((k_trace_single<false, true, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+        else XGB_LAUNCH((k_trace_single<false, false, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     } else if (flat && sc.blasLayout == 0) {
         if (count) XGB_LAUNCH((k_trace_flat2<false, true, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
         else XGB_LAUNCH((k_trace_flat2<false, false, OneScene>))(OneScene{sc, none}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
@@ -760,11 +798,15 @@ void launchExtend(const SceneDev& sc, PathQueue q, HitQueue h, Ctrl* ctrl, int n
     }
 }
 void launchExtendBatch(const BatchView& b, PathQueue q, HitQueue h, Ctrl* ctrl, int numSMs, cudaStream_t s) {
-    if (b.flat) XGB_LAUNCH((k_trace_flat2<false, false, BatchScenes>))(BatchScenes{b}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    if (b.flat == kBatchSingle)
+        XGB_LAUNCH((k_trace_single<false, false, BatchScenes>))(BatchScenes{b}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
+    else if (b.flat) XGB_LAUNCH((k_trace_flat2<false, false, BatchScenes>))(BatchScenes{b}, q, h, ShadowQueue{}, PathQueue{}, ctrl);
     else XGB_LAUNCH(k_extend_batch)(b, q, h, ctrl);
 }
 void launchShadowBatch(const BatchView& b, ShadowQueue sq, PathQueue out, Ctrl* ctrl, int numSMs, cudaStream_t s) {
-    if (b.flat) XGB_LAUNCH((k_trace_flat2<true, false, BatchScenes>))(BatchScenes{b}, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    if (b.flat == kBatchSingle)
+        XGB_LAUNCH((k_trace_single<true, false, BatchScenes>))(BatchScenes{b}, PathQueue{}, HitQueue{}, sq, out, ctrl);
+    else if (b.flat) XGB_LAUNCH((k_trace_flat2<true, false, BatchScenes>))(BatchScenes{b}, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else XGB_LAUNCH(k_shadow_batch)(b, sq, out, ctrl);
 }
 
@@ -779,7 +821,7 @@ void launchShadow(const SceneDev& sc, const RenderParams& rp, ShadowQueue sq, Pa
     }
     if (flat && sc.blasLayout == 1) XGB_LAUNCH((k_trace_wide<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (sc.nInstances == 1 && sc.blasLayout == 0)
-        XGB_LAUNCH((k_trace_single<true, false>))(sc, rp, PathQueue{}, HitQueue{}, sq, out, ctrl);
+        XGB_LAUNCH((k_trace_single<true, false, OneScene>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else if (flat && sc.blasLayout == 0)
         XGB_LAUNCH((k_trace_flat2<true, false, OneScene>))(OneScene{sc, rp}, PathQueue{}, HitQueue{}, sq, out, ctrl);
     else XGB_LAUNCH(k_shadow)(sc, rp, sq, out, ctrl);

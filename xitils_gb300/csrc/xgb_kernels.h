@@ -144,12 +144,14 @@ struct RenderParams {
 
 // Device arrays of a batch of render jobs sharing one wavefront (xgb_render_batch):
 // a path of job j carries j << 24 | pixel in its pixel field.
+constexpr int kBatchFlat = 1, kBatchSingle = 2;
 struct BatchView {
     const SceneDev* scenes;
     const RenderParams* params;
     const unsigned long long* start;  // nJobs + 1 prefix sums of the jobs' path counts
     int nJobs;
-    int flat;    // every scene has <= 16 instances and binary mesh BVHs: the persistent per-lane kernels
+    int flat;    // kBatchFlat: every scene has <= 16 instances and binary mesh BVHs (the persistent per-lane
+                 // kernels); kBatchSingle: every scene is one instance of a binary mesh BVH; 0: general
     int nested;  // some scene has a material that evaluates another (the shade kernel with that code)
 };
 void launchGenerateBatch(const BatchView& b, PathQueue q, Ctrl* ctrl, int grid, cudaStream_t s);
