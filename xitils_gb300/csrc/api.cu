@@ -1076,7 +1076,11 @@ xgb_status xgb_scene_build(xgb_scene* s, void* stream) {
     sd.stackLimit = s->stackLimit;
     sd.shell = anyShell;
     sd.nested = 0;
-    for (const Material& m : dm) sd.nested |= (m.kind == MAT_MF_NORMALMAP ? 1 : 0) | (m.kind == MAT_MULTILOBE_SVBRDF ? 2 : 0);
+    sd.kinds = 0;
+    for (const Material& m : dm) {
+        sd.nested |= (m.kind == MAT_MF_NORMALMAP ? 1 : 0) | (m.kind == MAT_MULTILOBE_SVBRDF ? 2 : 0);
+        sd.kinds |= 1 << m.kind;
+    }
     sd.instBox = dBox;
     sd.materials = dMat;
     sd.textures = dTex;

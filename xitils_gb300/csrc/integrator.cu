@@ -143,10 +143,17 @@ void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQu
     case 1: launchShadeMask1(job, in, h, out, sq, ctrl, numSMs, s); break;
     case 2: launchShadeMask2(job, in, h, out, sq, ctrl, numSMs, s); break;
     case 3: launchShadeMask3(job, in, h, out, sq, ctrl, numSMs, s); break;
-    default:
+    default: {
+        // plain renders of scenes whose non-emissive materials are all Lambert or all GGX metal
+        // take a variant with only that material's code
+        const int basic = sc.kinds & ~(1 << MAT_EMISSION);
         if (rp.guided || rp.train || rp.aov) launchShadeVariant<OneJob, 0, true>(job, in, h, out, sq, ctrl, numSMs, s);
+        else if (basic == (1 << MAT_METAL)) launchShadeVariant<OneJob, kOnlyMetal, false>(job, in, h, out, sq, ctrl, numSMs, s);
+        else if (basic == (1 << MAT_DIFFUSE))
+            launchShadeVariant<OneJob, kOnlyDiffuse, false>(job, in, h, out, sq, ctrl, numSMs, s);
         else launchShadeVariant<OneJob, 0, false>(job, in, h, out, sq, ctrl, numSMs, s);
         break;
+    }
     }
 }
 

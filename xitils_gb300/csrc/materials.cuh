@@ -271,7 +271,28 @@ __device__ __forceinline__ float metalRoughness(const SceneDev& sc, const Materi
     return texLookup(sc.textures[m.tex], s.uv.x, s.uv.y).x;
 }
 
+// Shade-kernel variants for scenes whose non-emissive materials are all of one
+// kind carry only that kind's code: VARIANT bits 8 and 9 (kOnlyDiffuse,
+// kOnlyMetal) restrict the basic material switch, bits 0 and 1 are the nested
+// materials (see bsdfCosT below). kindOn<V>(k): the code of kind k is compiled in.
+constexpr int kOnlyDiffuse = 0x100, kOnlyMetal = 0x200;
+template <int V>
+__device__ __forceinline__ constexpr bool kindOn(int k) {
+    return (V & kOnlyDiffuse) ? k == MAT_DIFFUSE : (V & kOnlyMetal) ? k == MAT_METAL : true;
+}
+
+template <int V = 0>
 __device__ __forceinline__ V3 bsdfCosBasic(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    if (V & kOnlyDiffuse) {
+        V3 a = V3(m.albedo.x, m.albedo.y, m.albedo.z) / kPi;
+        if (m.tex >= 0) a = a * texLookup(sc.textures[m.tex], s.uv.x, s.uv.y);
+        return m.kind == MAT_DIFFUSE ? a * clampPositive(dot(s.sn, wi)) : V3();
+    }
+    if (V & kOnlyMetal) {
+        if (m.kind != MAT_METAL) return V3();
+        float r = metalRoughness(sc, m, s);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z), (m.flags & 1) != 0}.bsdfCos(s, wi);
+    }
     switch (m.kind) {
     case MAT_DIFFUSE: {  // Material.h:59-65
         V3 a = V3(m.albedo.x, m.albedo.y, m.albedo.z) / kPi;
@@ -291,7 +312,14 @@ __device__ __forceinline__ V3 bsdfCosBasic(const SceneDev& sc, const Material& m
     }
 }
 
+template <int V = 0>
 __device__ __forceinline__ float pdfBasic(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
+    if (V & kOnlyDiffuse) return m.kind == MAT_DIFFUSE ? clampPositive(dot(wi, s.sn)) / kPi : 0.0f;
+    if (V & kOnlyMetal) {
+        if (m.kind != MAT_METAL) return 0.0f;
+        float r = metalRoughness(sc, m, s);
+        return MetalD{r * r, V3(m.albedo.x, m.albedo.y, m.albedo.z), (m.flags & 1) != 0}.pdf(s, wi);
+    }
     switch (m.kind) {
     case MAT_DIFFUSE: return clampPositive(dot(wi, s.sn)) / kPi;  // Material.h:78-81
     case MAT_METAL: {
@@ -307,9 +335,15 @@ __device__ __forceinline__ float pdfBasic(const SceneDev& sc, const Material& m,
     }
 }
 
+template <int V = 0>
 __device__ __forceinline__ V3 sampleBasic(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3* wi,
                                           float* pdf) {
-    switch (m.kind) {
+    if ((V & (kOnlyDiffuse | kOnlyMetal)) && !kindOn<V>(m.kind)) {  // not in the scene: never reached
+        *wi = s.sn;
+        *pdf = 0.0f;
+        return V3();
+    }
+    switch ((V & kOnlyDiffuse) ? (int)MAT_DIFFUSE : (V & kOnlyMetal) ? (int)MAT_METAL : m.kind) {
     case MAT_DIFFUSE: {  // Material.h:67-76, Vector.h:817-824
         Basis basis(s.sn);
         float u = rng.randf() * 1.0f;
@@ -506,21 +540,23 @@ __device__ __forceinline__ V3 albedoOf(const SceneDev& sc, const Material& m, co
 
 // Material dispatch (Material.h:9-48). NESTED is a mask of the materials that
 // evaluate another material which the code is compiled for: 1 microfacet normal
-// mapping, 2 MultiLobeSVBRDF. The shade kernel is instantiated per mask so that a
-// scene only carries the code (and registers) of the materials it has.
+// mapping, 2 MultiLobeSVBRDF; with kOnlyDiffuse or kOnlyMetal (and no nested
+// material) the basic switch holds that one kind. The shade kernel is
+// instantiated per mask so that a scene only carries the code (and registers)
+// of the materials it has.
 template <int NESTED>
 __device__ __forceinline__ V3 bsdfCosT(const SceneDev& sc, const Material& m, const Surface& s, Pcg& rng, V3 wi) {
     if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:489-491
         return bsdfCosBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), wi);
     if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return bsdfCosMfnm(sc, m, s, rng, wi);
-    return bsdfCosBasic(sc, m, s, wi);
+    return bsdfCosBasic<NESTED>(sc, m, s, wi);
 }
 template <int NESTED>
 __device__ __forceinline__ float getPDFT(const SceneDev& sc, const Material& m, const Surface& s, V3 wi) {
     if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:497-499, divided by the double M_PI
         return (float)((double)clampPositive(dot(s.sn, wi)) / kPiD);
     if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return getPDFMfnm(sc, m, s, wi);
-    return pdfBasic(sc, m, s, wi);
+    return pdfBasic<NESTED>(sc, m, s, wi);
 }
 // Returns material_eval = f * cos / pdf and samples wi (Material.h:22-28).
 // *pdf is left untouched where the reference leaves it untouched.
@@ -530,7 +566,7 @@ __device__ __forceinline__ V3 evalAndSampleT(const SceneDev& sc, const Material&
     if ((NESTED & 2) && m.kind == MAT_MULTILOBE_SVBRDF)  // Main.cpp:493-495
         return sampleBasic(sc, sc.materials[m.base], svbrdfPerturb(sc, m, s, rng), rng, wi, pdf);
     if ((NESTED & 1) && m.kind == MAT_MF_NORMALMAP) return evalAndSampleMfnm(sc, m, s, rng, wi, pdf);
-    return sampleBasic(sc, m, s, rng, wi, pdf);
+    return sampleBasic<NESTED>(sc, m, s, rng, wi, pdf);
 }
 
 // SurfaceIntersection of a hit (TriangleIndexed.h:128-171 + Object.h:44-85).

@@ -183,9 +183,14 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
 // shading 12.6 instead of 15.0 ms per render at two blocks, the guided room 82.5
 // instead of 79.9 Mpaths/s, the Cornell box 2.03 instead of 1.98 ms; with nested
 // materials two blocks (128 registers, 60-90 bytes of spills) -- the
-// normal-mapping scene 101 instead of 88 Mpaths/s at one block (140 registers).
+// normal-mapping scene 101 instead of 88 Mpaths/s at one block (140 registers);
+// the GGX-metal-only variant four blocks (64 registers, ~200 bytes of spills) --
+// terrain shading 10.1 instead of 11.6 ms per render at three, 1762 against 1834
+// Mpaths/s -- while the Lambert-only variant stays at three (the Cornell box
+// 9.5 against 9.9 ms of shading over five renders at four, the room 40.8
+// against 42.2).
 template <class J, int NESTED, bool EXTRAS>
-__global__ void __launch_bounds__(kShadeBlock, NESTED ? 2 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
+__global__ void __launch_bounds__(kShadeBlock, (NESTED & 3) ? 2 : (NESTED & kOnlyMetal) ? 4 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
                                                        ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
     const int lane = threadIdx.x & 31;

@@ -162,6 +162,7 @@ struct SceneDev {
     int fixes;       // opt-in quirk fixes of the render (XGB_FIX_DROP_NONFINITE = 2)
     int shell;       // 1 when some mesh is shell-mapped (its hits can be discarded during traversal)
     int nested;      // materials that evaluate another: bit 0 microfacet normal mapping, bit 1 MultiLobeSVBRDF
+    int kinds;       // bit k: some material of the scene is of MaterialKind k
     // Device-side traversal bounds (xgb_scene_set_traversal_limits): a ray whose
     // traversal takes more than maxSteps loop steps sets error bit 4 and ends; a
     // push onto a stack already holding stackLimit entries sets error bit 1 and
