@@ -185,7 +185,7 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
 // materials two blocks (128 registers, 60-90 bytes of spills) -- the
 // normal-mapping scene 101 instead of 88 Mpaths/s at one block (140 registers);
 // the GGX-metal-only variant four blocks (64 registers, ~200 bytes of spills) --
-// terrain shading 10.1 instead of 11.6 ms per render at three, 1762 against 1834
+// terrain shading 10.1 instead of 11.6 ms per render at three, 1834 instead of 1762
 // Mpaths/s -- while the Lambert-only variant stays at three (the Cornell box
 // 9.5 against 9.9 ms of shading over five renders at four, the room 40.8
 // against 42.2).

@@ -333,6 +333,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
                                                             PathQueue out, Ctrl* ctrl) {
     const unsigned int n = ANY ? ctrl->nShadow : ctrl->nActive;
     unsigned int* head = ANY ? &ctrl->shadowHead : &ctrl->extendHead;
+    constexpr bool kBatch = !std::is_same<S, OneScene>::value;
+    int rayMaxSteps = 0, rayStack = 0;  // a batch: the current ray's job's bounds
     int job = 0;
     int nInst = 0;
     const int lane = threadIdx.x & 31;
@@ -375,6 +377,10 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             br = BoxRay{wo.x, wo.y, wo.z, 1.0f / wd.x, 1.0f / wd.y, 1.0f / wd.z};
             job = scenes.jobOf(ANY ? __float_as_uint(d4.w) : __float_as_uint(q.thr[ray].w));
             nInst = scenes.scene(job).nInstances;
+            if (kBatch) {  // the job's traversal bounds, read once per ray
+                rayMaxSteps = scenes.scene(job).maxSteps;
+                rayStack = min(kStackDepth, scenes.scene(job).stackLimit);
+            }
             hit.prim = -1;
             hit.inst = -1;
             hit.t = tMax;
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             if (m.rootIsLeaf) { leafAddr = m.rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > scenes.scene(job).maxSteps) {
+        if (guard > (kBatch ? rayMaxSteps : scenes.scene(0).maxSteps)) {
             atomicOr(&ctrl->errors, 4u);
             nodeAddr = kSentinel;
             leafAddr = 0;
@@ -437,7 +443,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_flat2(S scenes, PathQueue
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= kStackDepth || sp >= scenes.scene(job).stackLimit) {
+                if (sp >= (kBatch ? rayStack : min(kStackDepth, scenes.scene(0).stackLimit))) {
                     atomicOr(&ctrl->errors, 1u);
                     sp = 0;
                     nodeAddr = kSentinel;
@@ -537,6 +543,7 @@ __global__ void __launch_bounds__(kTraceBlock, SingleTraits<S>::kMinBlocks)
     const Node2* nodes = m0.nodes2;
     const TriV* tris = m0.tris;
     int job = 0;
+    int rayMaxSteps = 0, rayStack = 0;  // a batch: the current ray's job's bounds
     const int lane = threadIdx.x & 31;
     const unsigned int ltMask = (1u << lane) - 1u;
     int stack[kStackDepth];
@@ -571,6 +578,8 @@ __global__ void __launch_bounds__(kTraceBlock, SingleTraits<S>::kMinBlocks)
                 job = scenes.jobOf(ANY ? __float_as_uint(d4.w) : __float_as_uint(__ldg(&q.thr[ray].w)));
                 in = &scenes.scene(job).instances[0];
                 identity = in->identity != 0;
+                rayMaxSteps = scenes.scene(job).maxSteps;
+                rayStack = scenes.scene(job).stackLimit;
             }
             if (!identity) {
                 o = xformPointRn(in->matInv, o);
@@ -593,7 +602,11 @@ __global__ void __launch_bounds__(kTraceBlock, SingleTraits<S>::kMinBlocks)
             if (rootIsLeaf) { leafAddr = rootLeaf; nodeAddr = kSentinel; }
             else { leafAddr = 0; nodeAddr = 0; }
         }
-        if (guard > scenes.scene(job).maxSteps) { atomicOr(&ctrl->errors, 4u); nodeAddr = kSentinel; leafAddr = 0; }
+        if (guard > (kBatch ? rayMaxSteps : scenes.scene(0).maxSteps)) {
+            atomicOr(&ctrl->errors, 4u);
+            nodeAddr = kSentinel;
+            leafAddr = 0;
+        }
         bool searching = true;
         while ((unsigned int)nodeAddr < (unsigned int)kSentinel) {
             if (COUNT) wc.nodes++;
@@ -606,7 +619,12 @@ __global__ void __launch_bounds__(kTraceBlock, SingleTraits<S>::kMinBlocks)
             if (h0 && h1) {
                 int near = dd.x, far = dd.y;
                 if (t1 < t0) { near = dd.y; far = dd.x; }
-                if (sp >= scenes.scene(job).stackLimit) { atomicOr(&ctrl->errors, 1u); sp = 0; nodeAddr = kSentinel; break; }
+                if (sp >= (kBatch ? rayStack : scenes.scene(0).stackLimit)) {
+                    atomicOr(&ctrl->errors, 1u);
+                    sp = 0;
+                    nodeAddr = kSentinel;
+                    break;
+                }
                 stack[sp++] = far;
                 nodeAddr = near;
             } else if (h0) {
