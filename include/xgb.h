@@ -398,6 +398,12 @@ xgb_status xgb_guide_train_batch(xgb_guide* guide, int n, const float* pos, cons
  * pooled for the next call. The pool holds 2^22 records; a call that finds more
  * than max_steps_per_call batches drops the excess. */
 xgb_status xgb_guide_set_training(xgb_guide* guide, int batch_rows, int max_steps_per_call, int product_target);
+/* Polls of each mbarrier wait of the network's tensor-core inference before it
+ * gives up (default 2^22; no counterpart in the reference). A wait that gives
+ * up makes the call return XGB_DEVICE_TIMEOUT after the kernel has waited
+ * (with the default bound) for its matrix operations in flight and freed its
+ * tensor memory; the context stays usable. Tests set 0 to take that path. */
+xgb_status xgb_guide_set_wait_limit(xgb_guide* guide, int polls);
 /* Adam steps taken so far (explicit and in-render). */
 xgb_status xgb_guide_train_steps(xgb_guide* guide, uint64_t* out);
 /* Guided rendering: at Diffuse / Metal / Glossy vertices xgb_render samples the BSDF

@@ -135,3 +135,45 @@ def test_limits_are_checked_on_the_host(api_mod):
         with pytest.raises(api.XgbError) as e:
             b.scene.set_traversal_limits(steps, stack)
         assert e.value.status == 1
+
+
+def test_tensor_core_inference_wait_runs_out(api_mod):
+    """The learned proposal's tcgen05 inference waits on an mbarrier for its
+    matrix operations; with the wait bound lowered to zero polls every wait gives
+    up at once: the kernel records ERR_WAIT (bit 8), waits with the default bound
+    for the operations it issued, frees its tensor memory and ends, and the call
+    returns XGB_DEVICE_TIMEOUT -- for the host-row entry point (xgb_guide_infer)
+    and for a guided render. With the bound restored, the same guide infers the
+    same outputs as before and the same render succeeds on the same context."""
+    api = api_mod
+    ctx = api.Context(0)
+    gd = api.Guide(ctx, seed=4)
+    gd.set_bounds([0, 0, 0], [1, 1, 1])
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0, 1, (300, 3)).astype(np.float32)
+    nrm = rng.normal(size=(300, 3)).astype(np.float32)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    wo = rng.normal(size=(300, 3)).astype(np.float32)
+    wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+    want = gd.infer(pos, nrm, wo)
+    gd.set_wait_limit(0)
+    with pytest.raises(api.XgbError) as e:
+        gd.infer(pos, nrm, wo)
+    assert e.value.status == XGB_DEVICE_TIMEOUT
+    desc = scenes.occluded_room(32, 32, 2)
+    b = api.load_scene(ctx, desc)
+    b.scene.setGuide(gd, 0.5, train=False)
+    rt = api.RenderTarget(ctx, desc.width, desc.height)
+    with pytest.raises(api.XgbError) as e:
+        rt.render(b.scene, desc.spp, desc.params)
+    assert e.value.status == XGB_DEVICE_TIMEOUT
+    assert b.scene.stats()["error_flags"] & 8
+    gd.set_wait_limit()
+    np.testing.assert_array_equal(gd.infer(pos, nrm, wo), want)
+    rt.clear()
+    rt.render(b.scene, desc.spp, desc.params)
+    st = b.scene.stats()
+    assert st["error_flags"] == 0 and st["paths"] == desc.n_paths
+    assert np.isfinite(rt.download()).all()
+    with pytest.raises(api.XgbError):
+        gd.set_wait_limit(-1)

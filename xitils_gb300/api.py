@@ -142,6 +142,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "xgb_guide_sample": [P, C.c_int, FP, FP, FP, C.c_uint32, FP, FP],
         "xgb_guide_train_batch": [P, C.c_int, FP, FP, FP, FP, FP, FP, C.c_float, FP],
         "xgb_guide_set_training": [P, C.c_int, C.c_int, C.c_int],
+        "xgb_guide_set_wait_limit": [P, C.c_int],
         "xgb_guide_train_steps": [P, C.POINTER(C.c_uint64)],
         "xgb_scene_set_guide": [P, P, C.c_float, C.c_int, C.c_float],
     }
@@ -670,6 +671,10 @@ class Guide:
         self.ctx.check(self.ctx.lib.xgb_guide_sample(self.h, n, _fp(pos), _fp(nrm), _fp(wo), seed, _fp(dirs), _fp(pdf)),
                        "sample")
         return dirs, pdf
+
+    def set_wait_limit(self, polls: int = 1 << 22):
+        """Polls of each tensor-core inference wait before it gives up (tests: 0)."""
+        self.ctx.check(self.ctx.lib.xgb_guide_set_wait_limit(self.h, int(polls)), "set_wait_limit")
 
     def set_training(self, batch_rows: int = 8192, max_steps_per_call: int = 512, product: bool = True):
         self.ctx.check(self.ctx.lib.xgb_guide_set_training(self.h, batch_rows, max_steps_per_call, int(product)),

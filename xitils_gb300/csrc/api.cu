@@ -1387,10 +1387,11 @@ xgb_status xgb_render(xgb_scene* s, const xgb_integrator_params* params, xgb_fil
             }
         }
         const Ctrl& c = *s->ctrlHost;
+        if (c.errors) break;  // a device bound ran out: the call returns its status below
         if (c.nextPath >= c.totalPaths && c.nOut == 0) break;
         if (guard > (1 << 22)) return fail(ctx, XGB_DEVICE_TIMEOUT, "xgb_render: wavefront did not drain");
     }
-    if (gd && rp.train) {
+    if (gd && rp.train && s->ctrlHost->errors == 0) {
         if (prof) cudaEventRecord(s->events[kEv * kIterPerCheck], st);
         // every path of the call has finished: records take their incident
         // radiance, those that carry some join the pool, and the pool is
@@ -1602,6 +1603,7 @@ xgb_status xgb_guide_create(xgb_ctx* ctx, uint32_t seed, xgb_guide** out) {
     GuideDevice& g = gd->g;
     g.maxRows = 65536;
     g.step = 0;
+    g.waitLimit = 1 << 22;
     const int R = g.maxRows;
     auto alloc = [&](size_t bytes) -> void* {
         void* p = nullptr;
@@ -1806,6 +1808,14 @@ xgb_status xgb_guide_train_batch(xgb_guide* gd, int n, const float* pos, const f
     XGB_CUDA(ctx, cudaStreamSynchronize(st));
     XGB_CUDA(ctx, cudaGetLastError());
     if (loss) *loss = sc[1];
+    return XGB_OK;
+}
+
+xgb_status xgb_guide_set_wait_limit(xgb_guide* gd, int polls) {
+    if (!gd) return XGB_INVALID_ARG;
+    if (polls < 0) return fail(gd->ctx, XGB_INVALID_ARG, "xgb_guide_set_wait_limit: polls >= 0");
+    XGB_CUDA(gd->ctx, cudaStreamSynchronize(gd->ctx->stream));
+    gd->g.waitLimit = polls;
     return XGB_OK;
 }
 

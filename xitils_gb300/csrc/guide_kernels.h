@@ -34,6 +34,7 @@ struct GuideDevice {
     GuideWeights w;
     GuideScratch scratch;
     int maxRows;  // training batch capacity (multiple of 64)
+    int waitLimit;  // polls of a tensor-memory inference wait before it gives up (xgb_guide_set_wait_limit)
     int step;     // Adam step count
     // training pool filled by the wavefront (records with non-zero radiance)
     GuideRecord* pool;

@@ -28,6 +28,7 @@
 // group walks its tiles with a grid stride.
 //
 // Waits are bounded: an mbarrier wait that does not complete within its limit
+// (GuideDevice::waitLimit polls, 2^22 unless a test lowers it)
 // is voted on by the group, sets ERR_WAIT in the launch's error word (the render
 // returns XGB_DEVICE_TIMEOUT), waits once more (bounded) for the group's MMAs in
 // flight and leaves the group's loop; the CTA then frees its TMEM columns.
@@ -46,7 +47,7 @@ constexpr int kTcThreads = kTcRows * kTcGroups;
 constexpr int kTcCols = 64 * kTcGroups;        // TMEM columns allocated: 64 FP32 accumulators per group
 constexpr int kTcCtasPerSm = 3;                // launch = SMs x this x waves
 constexpr int kTcWaves = 2;
-constexpr int kTcWaitLimit = 1 << 22;
+constexpr int kTcWaitLimit = 1 << 22;  // polls of the wait for MMAs in flight after a timeout
 
 struct __align__(1024) TcSmem {
     __nv_bfloat16 w[3][64 * 64];                   // layers 0-2 (B operands, core-matrix layout)
@@ -123,9 +124,9 @@ __device__ __forceinline__ void commit(uint32_t mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-// Bounded wait for the mbarrier phase of the given parity.
-__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity) {
-    for (int it = 0; it < kTcWaitLimit; ++it) {
+// Bounded wait for the mbarrier phase of the given parity: at most `limit` polls.
+__device__ __forceinline__ bool mbarWait(uint32_t mbar, uint32_t parity, int limit = kTcWaitLimit) {
+    for (int it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -218,7 +219,7 @@ __device__ __forceinline__ void tcTeardown(TcSmem& S) {
 // (the whole group agrees).
 template <int N>
 __device__ __forceinline__ bool tcLayer(TcSmem& S, int group, const __nv_bfloat16* B, uint32_t& parity,
-                                        float (&out)[64], const float* bias) {
+                                        float (&out)[64], const float* bias, int waitLimit) {
     fenceProxyAsync();  // the operand stores become visible to the tensor cores
     tcFenceBefore();
     groupSync(group);
@@ -231,7 +232,7 @@ __device__ __forceinline__ bool tcLayer(TcSmem& S, int group, const __nv_bfloat1
         for (int j = 0; j < 4; ++j) mma(tmem, matDesc(a0 + 256u * j), matDesc(b0 + 256u * j), instrDesc<N>(), j > 0);
         commit(mbar);
     }
-    const bool done = mbarWait(mbar, parity);
+    const bool done = mbarWait(mbar, parity, waitLimit);
     parity ^= 1u;
     if (!groupAll(group, done)) return false;
     tcFenceAfter();
@@ -250,16 +251,17 @@ __device__ __forceinline__ bool tcLayer(TcSmem& S, int group, const __nv_bfloat1
 // The four layers for the group's tile, whose features are in its A operand;
 // row r's 40 outputs in y (the first kGuideOut of 48). Returns false on a
 // timed-out wait.
-__device__ __forceinline__ bool tcForward(TcSmem& S, int group, int r, uint32_t& parity, float (&y)[64]) {
+__device__ __forceinline__ bool tcForward(TcSmem& S, int group, int r, uint32_t& parity, float (&y)[64],
+                                          int waitLimit) {
     float h[64];
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
-        if (!tcLayer<64>(S, group, S.w[l], parity, h, S.bias + 64 * l)) return false;
+        if (!tcLayer<64>(S, group, S.w[l], parity, h, S.bias + 64 * l, waitLimit)) return false;
 #pragma unroll
         for (int k = 0; k < 64; ++k) h[k] = fmaxf(h[k], 0.0f);
         storeRow(S.a[group], r, h);
     }
-    return tcLayer<kGuideOutPad>(S, group, S.w3, parity, y, S.bias + 192);
+    return tcLayer<kGuideOutPad>(S, group, S.w3, parity, y, S.bias + 192, waitLimit);
 }
 
 // After a timed-out wait: the error bit, then a bounded second wait for the
@@ -272,7 +274,7 @@ __device__ __forceinline__ void tcAbort(TcSmem& S, int group, uint32_t parity, u
 // Rows of feature vectors (xgb_guide_infer / xgb_guide_sample): X0 [rows][64]
 // BF16, Y [rows][48] FP32.
 __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_inferRowsTc(const __nv_bfloat16* X0, int rows, GuideWeights w,
-                                                            float* Y, unsigned int* errors) {
+                                                            float* Y, unsigned int* errors, int waitLimit) {
     extern __shared__ unsigned char tcRaw[];
     TcSmem& S = *reinterpret_cast<TcSmem*>(tcRaw);
     tcSetup(S, w);
@@ -288,7 +290,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_inferRowsTc(const 
             *reinterpret_cast<uint4*>(dst + coreOffset(r, 8 * g)) = v;
         }
         float y[64];
-        if (!tcForward(S, group, r, parity, y)) {
+        if (!tcForward(S, group, r, parity, y, waitLimit)) {
             tcAbort(S, group, parity, errors);
             break;
         }
@@ -302,12 +304,15 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_inferRowsTc(const 
 // Per-path inference of the wavefront: each hit of the input queue gets its
 // 8-lobe mixture (10 float4: the lobes' (mu, kappa), then the 8 weights).
 __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_inferPathsTc(SceneDev sc, GuideWeights w, GuideBounds gb, PathQueue q,
-                                                             HitQueue h, Ctrl* ctrl, float4* mix) {
+                                                             HitQueue h, Ctrl* ctrl, float4* mix, int waitLimit) {
     extern __shared__ unsigned char tcRaw[];
     TcSmem& S = *reinterpret_cast<TcSmem*>(tcRaw);
+    const unsigned int n = ctrl->nActive;
+    // CTAs without a tile (the short queues at the end of a render) leave before
+    // allocating TMEM and staging the weights
+    if (blockIdx.x * (unsigned int)(kTcGroups * kTcRows) >= n) return;
     tcSetup(S, w);
     uint32_t parity = 0;
-    const unsigned int n = ctrl->nActive;
     const int group = threadIdx.x / kTcRows, r = threadIdx.x & (kTcRows - 1);
     const unsigned int stride = gridDim.x * (unsigned int)(kTcGroups * kTcRows);
     for (unsigned int base = (blockIdx.x * kTcGroups + group) * (unsigned int)kTcRows; base < n; base += stride) {
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcCtasPerSm) k_inferPathsTc(Scene
             for (int k = 0; k < 64; ++k) f[k] = 0.0f;
         storeRow(S.a[group], r, f);
         float y[64];
-        if (!tcForward(S, group, r, parity, y)) {
+        if (!tcForward(S, group, r, parity, y, waitLimit)) {
             tcAbort(S, group, parity, &ctrl->errors);
             break;
         }
@@ -370,13 +375,13 @@ void guideInferRows(const GuideDevice& g, const __nv_bfloat16* X0, int rowsPad, 
     int grid = (groups + kTcGroups - 1) / kTcGroups;
     if (gLaunchCtas > 0 && grid > gLaunchCtas) grid = gLaunchCtas;
     k_inferRowsTc<<<grid > 0 ? grid : 1, kTcThreads, sizeof(TcSmem), s>>>(
-        X0, rowsPad, g.w, Y, reinterpret_cast<unsigned int*>(g.scratch.scalars + 2));
+        X0, rowsPad, g.w, Y, reinterpret_cast<unsigned int*>(g.scratch.scalars + 2), g.waitLimit);
 }
 
 void guideInferPaths(const SceneDev& sc, const GuideDevice& g, GuideBounds gb, PathQueue q, HitQueue h, Ctrl* ctrl,
                      float4* mix, int grid, cudaStream_t s) {
     if (gLaunchCtas > 0) grid = gLaunchCtas;
-    k_inferPathsTc<<<grid, kTcThreads, sizeof(TcSmem), s>>>(sc, g.w, gb, q, h, ctrl, mix);
+    k_inferPathsTc<<<grid, kTcThreads, sizeof(TcSmem), s>>>(sc, g.w, gb, q, h, ctrl, mix, g.waitLimit);
 }
 
 }  // namespace xgb
