@@ -276,6 +276,9 @@ __device__ __forceinline__ float metalRoughness(const SceneDev& sc, const Materi
 // kOnlyMetal) restrict the basic material switch, bits 0 and 1 are the nested
 // materials (see bsdfCosT below). kindOn<V>(k): the code of kind k is compiled in.
 constexpr int kOnlyDiffuse = 0x100, kOnlyMetal = 0x200;
+// VARIANT bit 10: the scene has no emissive material (and so no lights): the
+// shade kernel leaves out emission and next-event estimation.
+constexpr int kNoEmitters = 0x400;
 template <int V>
 __device__ __forceinline__ constexpr bool kindOn(int k) {
     return (V & kOnlyDiffuse) ? k == MAT_DIFFUSE : (V & kOnlyMetal) ? k == MAT_METAL : true;
