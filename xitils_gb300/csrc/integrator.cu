@@ -144,11 +144,12 @@ void launchShade(const SceneDev& sc, const RenderParams& rp, PathQueue in, HitQu
     case 2: launchShadeMask2(job, in, h, out, sq, ctrl, numSMs, s); break;
     case 3: launchShadeMask3(job, in, h, out, sq, ctrl, numSMs, s); break;
     default: {
-        // plain renders of scenes whose non-emissive materials are all Lambert or all GGX metal
-        // take a variant with only that material's code
+        // plain renders (standard integrator) of scenes whose non-emissive materials are all
+        // Lambert or all GGX metal take a variant with only that material's code
         const int basic = sc.kinds & ~(1 << MAT_EMISSION);
         const bool emitters = (sc.kinds & (1 << MAT_EMISSION)) != 0 || sc.nLights > 0;
         if (rp.guided || rp.train || rp.aov) launchShadeVariant<OneJob, 0, true>(job, in, h, out, sq, ctrl, numSMs, s);
+        else if (rp.integrator != 0) launchShadeVariant<OneJob, 0, false>(job, in, h, out, sq, ctrl, numSMs, s);
         else if (basic == (1 << MAT_METAL) && !emitters)
             launchShadeVariant<OneJob, kOnlyMetal | kNoEmitters, false>(job, in, h, out, sq, ctrl, numSMs, s);
         else if (basic == (1 << MAT_METAL)) launchShadeVariant<OneJob, kOnlyMetal, false>(job, in, h, out, sq, ctrl, numSMs, s);

@@ -188,10 +188,11 @@ __device__ __forceinline__ void loadMixture(const float4* m, VmfMixture& mx) {
 // terrain shading 10.1 instead of 11.6 ms per render at three, 1834 instead of 1762
 // Mpaths/s -- while the Lambert-only variant stays at three (the Cornell box
 // 9.5 against 9.9 ms of shading over five renders at four, the room 40.8
-// against 42.2). Without emitters (no emission, no NEE code) the metal variant
-// shades the terrain in 9.4 ms per render (1866 Mpaths/s), 9.37 at five blocks.
+// against 42.2). Without emitters (no emission, no NEE code) and with the
+// standard integrator only, the metal variant shades the terrain in 9.2 ms per
+// render at four blocks (1878 Mpaths/s) and 9.1 ms at five (51 registers, 1884).
 template <class J, int NESTED, bool EXTRAS>
-__global__ void __launch_bounds__(kShadeBlock, (NESTED & 3) ? 2 : (NESTED & kOnlyMetal) ? 4 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
+__global__ void __launch_bounds__(kShadeBlock, (NESTED & 3) ? 2 : (NESTED & kNoEmitters) ? 5 : (NESTED & kOnlyMetal) ? 4 : 3) k_shade(J jobs, PathQueue in, HitQueue hq, PathQueue out,
                                                        ShadowQueue sq, Ctrl* ctrl) {
     const unsigned int n = ctrl->nActive;
     const int lane = threadIdx.x & 31;
@@ -221,7 +222,8 @@ __global__ void __launch_bounds__(kShadeBlock, (NESTED & 3) ? 2 : (NESTED & kOnl
             jobs.decode(packed, job, pix);
             const SceneDev& sc = jobs.scene(job);
             const RenderParams& rp = jobs.params(job);
-            const bool naive = rp.integrator == 1;
+            // the one-kind variants run the standard integrator only
+            const bool naive = !(NESTED & (kOnlyMetal | kOnlyDiffuse)) && rp.integrator == 1;
             const float pdfPrev = o4.w;
             V3 dir(d4.x, d4.y, d4.z);
             V3 thr(t4.x, t4.y, t4.z);
