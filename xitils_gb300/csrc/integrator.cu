@@ -71,11 +71,11 @@ __device__ __forceinline__ void groupedSample(unsigned long long local, unsigned
     const unsigned int full = (spp / G) * G;
     const unsigned long long grouped = (unsigned long long)full * px;
     if (local < grouped) {
-        const unsigned long long pass = (unsigned long long)px * G;
+        const unsigned long long pass = (unsigned long long)px * G;  // may exceed 2^32
         const unsigned int grp = (unsigned int)(local / pass);
-        const unsigned int r = (unsigned int)(local - (unsigned long long)grp * pass);
-        pix = r / G;
-        sample = grp * G + r % G;
+        const unsigned long long r = local - (unsigned long long)grp * pass;
+        pix = (unsigned int)(r / G);
+        sample = grp * G + (unsigned int)(r % G);
     } else {
         const unsigned long long t = local - grouped;
         sample = full + (unsigned int)(t / px);
